@@ -1,0 +1,179 @@
+/*
+ * qmprs_gb300 — C ABI of the GB300 (sm_103a) MPS-encoding library.
+ *
+ * The library replaces the numerical core of the reference project
+ * Qualition/qmprs (pure Python over quimb/numpy) behind its own Python API
+ * (qmprs_gb300.primitives.MPS, qmprs_gb300.synthesis.mps_encoding.Sequential).
+ * Every entry point below names the reference function it replaces.
+ *
+ * Conventions
+ *   - All buffers are DEVICE pointers owned by the caller unless stated;
+ *     sizes and offsets come from the plan (qmprs_plan_layout).
+ *   - Statevectors are complex64 (interleaved float re, im); amplitude index
+ *     bit (n-1-q) is qubit q (the reference's MSB order).
+ *   - Gates, MPS tensors and fidelities are complex128 / double.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     stream-ordered; a call returns after its work is enqueued, except where
+ *     it says it synchronises.
+ *   - Return value: QMPRS_OK or an error code; qmprs_last_error() gives the
+ *     message.  Error classes mirror the reference's exceptions: INVALID
+ *     maps to ValueError/TypeError, NONUNITARY to the ValueError raised at
+ *     qmprs/primitives/mps.py:837-839.
+ *   - One handle per host thread; handles hold no global state.
+ */
+#ifndef QMPRS_GB300_H
+#define QMPRS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QMPRS_OK 0
+#define QMPRS_ERR_INVALID 1
+#define QMPRS_ERR_UNSUPPORTED 2
+#define QMPRS_ERR_CUDA 3
+#define QMPRS_ERR_NUMERIC 4
+#define QMPRS_ERR_NONUNITARY 5
+
+typedef struct qmprs_ctx* qmprs_handle_t;
+typedef struct qmprs_plan* qmprs_plan_t;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int qmprs_version(void);
+
+/* Number of kernel launches the library has issued in this process.
+ * No reference counterpart (instrumentation). */
+int64_t qmprs_launch_count(void);
+
+/*
+ * Per-kernel profiling of qmprs_optimize_layers (instrumentation, no
+ * reference counterpart).  When enabled, every launch of the three sweep
+ * kernel classes is bracketed by CUDA events on the caller's stream;
+ * qmprs_plan_profile returns, for kernel 0 (environment stream: peel the
+ * gate off the circuit state and accumulate the environment), 1 (target
+ * update), 2 (circuit rebuild) or 3 (environment reduce + polar update), the
+ * launches, the summed event time in ms and the algorithmic bytes moved
+ * (complex64 reads and writes of the states active in each launch; 0 for
+ * kernel 3).  Enabling resets the counters; profiling synchronises once per
+ * sweep.
+ */
+int qmprs_plan_set_profiling(qmprs_plan_t p, int enable);
+int qmprs_plan_profile(qmprs_plan_t p, int kernel, int64_t* launches, double* milliseconds, double* bytes);
+
+/* Create a handle on the current CUDA device. */
+int qmprs_create(qmprs_handle_t* out);
+void qmprs_destroy(qmprs_handle_t h);
+/* Message of the last failing call on this handle (never NULL). */
+const char* qmprs_last_error(qmprs_handle_t h);
+
+/*
+ * Plan a batch of `num_states` states with the given qubit counts (host
+ * array, 2 <= n <= 30), at most `max_layers` unitary layers and MPS bond
+ * dimension `max_bond`.  Allocates the plan's device scratch.
+ * Replaces: the per-call set-up the reference performs implicitly in
+ * MPSEncoder.prepare_state (qmprs/synthesis/mps_encoding/base.py:58-106);
+ * the reference encodes one state per call, the plan batches many.
+ */
+int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, int max_layers,
+                      int max_bond, qmprs_plan_t* out);
+void qmprs_plan_destroy(qmprs_plan_t p);
+
+/*
+ * Sizes (in elements) of the caller-owned buffers and per-state offsets
+ * (host arrays of num_states entries, any may be NULL):
+ *   vec_elems    complex64 elements of a statevector batch
+ *   gate_elems   complex128 elements of the gate store (16 per gate slot)
+ *   tensor_elems complex128 elements of the MPS tensor store
+ *   vec_off / gate_off / tensor_off   start of state b in those buffers
+ * The arity store has gate_elems / 16 int8 entries, the bond store
+ * num_states * (max_qubits + 1) int32 entries (see qmprs_plan_max_qubits).
+ */
+int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, int64_t* tensor_elems,
+                      int64_t* vec_off, int64_t* gate_off, int64_t* tensor_off);
+int qmprs_plan_max_qubits(qmprs_plan_t p);
+
+/*
+ * (a) Statevector -> MPS truncated to `max_bond` (<= the plan's), with the
+ * quimb default cutoff `cutoff` (1e-10, rsum2).  Writes the site tensors
+ * (l, p, r) of state b, site s at tensor_off[b] + s * 2 * chi_b^2 with
+ * chi_b = min(max_bond, 2^floor(n_b/2)), the bonds, and the dense
+ * statevector of the truncated MPS into `target`.
+ * Replaces: MPS.from_statevector (qmprs/primitives/mps.py:219-249), i.e.
+ * quimb MatrixProductState.from_dense + tensor_network_1d_compress.
+ */
+int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv, int max_bond, double cutoff, void* tensors,
+                               int* bonds, void* target, void* stream);
+
+/*
+ * Dense statevector of an MPS held in the plan's tensor layout (site s of
+ * state b at tensor_off[b] + s * 2 * chi_b^2, bonds as written by
+ * qmprs_mps_from_statevector; every bond <= 64).
+ * Replaces: MPS.to_statevector (qmprs/primitives/mps.py:252-270), i.e.
+ * quimb MatrixProductState.to_dense.
+ */
+int qmprs_mps_to_statevector(qmprs_plan_t p, const void* tensors, const int* bonds, void* out, void* stream);
+
+/*
+ * (b)+(c) Disentangling layers.  From the dense target (normalised inside),
+ * generates up to `num_layers` layers: bond-2 truncation + Ran completion,
+ * then the adjoint layer applied to the working state, stopping a state
+ * early when |<0|psi> - 1| <= (1 - fidelity_threshold) + 1e-5.  Writes the
+ * gates (generation order), their arity (1 or 2), the number of layers per
+ * state and the complex zero-state overlap after each layer
+ * (num_states x num_layers complex128).  Synchronises the stream.
+ * Replaces: Sequential._get_unitary_layers
+ * (qmprs/synthesis/mps_encoding/sequential.py:330-398) with
+ * MPS.generate_bond_D_unitary_layer (qmprs/primitives/mps.py:849-891),
+ * MPS.apply_unitary_layer(inverse=True) (mps.py:973-995) and
+ * MPS.fidelity_with_zero_state (mps.py:1020-1039).
+ */
+int qmprs_unitary_layers(qmprs_plan_t p, const void* target, int num_layers, double fidelity_threshold,
+                         void* gates, int8_t* arity, int* layers_out, void* layer_fid, void* stream);
+
+/*
+ * (d) Environment sweeps.  Runs up to `num_sweeps` sweeps over every gate
+ * (last to first) of each state, replacing each gate by the conjugate of the
+ * polar factor of its environment.  After each sweep writes
+ * |<target|C|0>| / ||target|| into sweep_fid[b * num_sweeps + s]; if
+ * stop_fidelity > 0 a state stops sweeping once it reaches it.
+ * sweeps_done[b] receives the number of sweeps run.  Synchronises the
+ * stream once per sweep when stop_fidelity > 0, otherwise at the end.
+ * Replaces: Sequential._optimize_unitary_layers and _sweep_unitary_layers
+ * (qmprs/synthesis/mps_encoding/sequential.py:400-541).
+ */
+int qmprs_optimize_layers(qmprs_plan_t p, const void* target, void* gates, const int8_t* arity,
+                          const int* num_layers, int num_sweeps, double stop_fidelity, double* sweep_fid,
+                          int* sweeps_done, void* stream);
+
+/*
+ * Dense circuit state C|0...0> of the stored layers (circuit order = reverse
+ * generation order).
+ * Replaces: Sequential._tensor_network_from_unitary_layers(...).to_dense()
+ * (qmprs/synthesis/mps_encoding/sequential.py:216-292, 443-447) and the
+ * statevector of the emitted circuit.
+ */
+int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, const int* num_layers,
+                        void* out, void* stream);
+
+/*
+ * Per-state inner products <a|b> (complex128 out[num_states]) in fp64.
+ * Replaces: the np.dot(conj(sv), sv') fidelity of the reference tests
+ * (tests/synthesis/mps_encoding/test_sequential_encoding.py:67).
+ */
+int qmprs_overlap(qmprs_plan_t p, const void* a, const void* b, void* out, void* stream);
+
+/*
+ * Apply the adjoint (inverse != 0) or the gate itself of one generated layer
+ * to a statevector batch, in the reference's order.
+ * Replaces: MPS.apply_unitary_layer (qmprs/primitives/mps.py:893-995).
+ */
+int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t* arity, int layer,
+                      int inverse, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMPRS_GB300_H */

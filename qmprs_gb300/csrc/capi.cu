@@ -1,0 +1,609 @@
+// C ABI of the library: handles, batch plans and the stage entry points.
+//
+// The host side here is the native runtime of the encoder: it owns the
+// per-plan device scratch and work tables, sequences the kernel launches of
+// every stage on the caller's stream, and turns kernel error flags into
+// status codes and messages.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "qmprs_gb300.h"
+
+struct qmprs_ctx {
+  int device = 0;
+  std::string err;
+};
+
+struct qmprs_plan {
+  qmprs_ctx* h = nullptr;
+  int B = 0, max_n = 0, max_layers = 0, max_bond = 0, ntiles = 0, tile_bits = 0;
+  std::vector<int> n;
+  std::vector<int64_t> vec_off, gate_off, tensor_off;
+  int64_t vec_total = 0, gate_total = 0, tensor_total = 0;
+  // device tables
+  int *d_n = nullptr, *d_tile_state = nullptr, *d_tile_idx = nullptr, *d_state_tile0 = nullptr,
+      *d_state_ntiles = nullptr, *d_ticket = nullptr, *d_err = nullptr;
+  int64_t *d_vec_off = nullptr, *d_gate_off = nullptr, *d_tensor_off = nullptr;
+  int* d_bond_init = nullptr;
+  // scratch
+  float2 *S0 = nullptr, *S1 = nullptr, *S2 = nullptr;
+  double2* partials = nullptr;
+  double2* tt_partials = nullptr;
+  double2 *gram = nullptr, *vsel = nullptr, *vsel2 = nullptr, *vwork = nullptr;
+  double2* site_t = nullptr;
+  int *bonds = nullptr, *active = nullptr, *nlayers = nullptr, *num_active = nullptr;
+  double* nuc = nullptr;
+  double2 *sq = nullptr, *tnorm = nullptr;
+  BatchDev bd;
+  // profiling of the sweep kernels (kernel classes: 0 environment stream,
+  // 1 target update, 2 circuit rebuild, 3 environment reduce + polar):
+  // launches, event time, algorithmic bytes
+  bool prof = false;
+  int64_t prof_launches[4] = {0, 0, 0, 0};
+  double prof_ms[4] = {0, 0, 0, 0};
+  double prof_bytes[4] = {0, 0, 0, 0};
+  std::vector<int> gates_per_state;
+};
+
+static std::atomic<long long> g_launches{0};
+
+void qm_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+
+int set_err(qmprs_ctx* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(qmprs_ctx* h, cudaError_t e, const char* what) {
+  return set_err(h, QMPRS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cuda_fail(p->h, _e, #call); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** ptr, int64_t count) {
+  if (count <= 0) count = 1;
+  return cudaMalloc(reinterpret_cast<void**>(ptr), sizeof(T) * (size_t)count);
+}
+
+int chi_eff_host(int chi, int n) {
+  const int cap = 1 << (n / 2);
+  return chi < cap ? chi : cap;
+}
+
+int check_kernel_errors(qmprs_plan* p, cudaStream_t s) {
+  CK(cudaGetLastError());
+  int flags = 0;
+  CK(cudaMemcpyAsync(&flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (flags & KERR_NONUNITARY)
+    return set_err(p->h, QMPRS_ERR_NONUNITARY, "All the generated unitaries must be unitary.");
+  if (flags & KERR_EIG_WIDTH)
+    return set_err(p->h, QMPRS_ERR_UNSUPPORTED,
+                   "a bond of the MPS exceeds the supported width (bond > 64)");
+  if (flags & KERR_NONFINITE) return set_err(p->h, QMPRS_ERR_NUMERIC, "non-finite environment in a sweep");
+  if (flags & KERR_BAD_GATE)
+    return set_err(p->h, QMPRS_ERR_INVALID, "a gate slot has an invalid arity or position (gates skipped)");
+  return QMPRS_OK;
+}
+
+int read_max_gates(qmprs_plan* p, const int* nlayers_dev, cudaStream_t s, int* max_gates) {
+  std::vector<int> L(p->B);
+  CK(cudaMemcpyAsync(L.data(), nlayers_dev, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int m = 0;
+  p->gates_per_state.assign(p->B, 0);
+  for (int b = 0; b < p->B; ++b) {
+    if (L[b] < 0 || L[b] > p->max_layers) return set_err(p->h, QMPRS_ERR_INVALID, "num_layers entry out of range");
+    p->gates_per_state[b] = L[b] * p->n[b];
+    m = std::max(m, L[b] * p->n[b]);
+  }
+  *max_gates = m;
+  return QMPRS_OK;
+}
+
+// Event pairs around launches of one kernel class; summed after a sync.
+struct ProfLog {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> cls;
+  void begin(bool on, cudaStream_t s) {
+    if (!on) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+  }
+  void end(bool on, int c, cudaStream_t s) {
+    if (!on) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+    cls.push_back(c);
+  }
+  void flush(qmprs_plan* p) {
+    if (ev.empty()) return;
+    cudaEventSynchronize(ev.back());
+    for (size_t i = 0; i < cls.size(); ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+      p->prof_ms[cls[i]] += ms;
+      p->prof_launches[cls[i]] += 1;
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    ev.clear();
+    cls.clear();
+  }
+};
+
+__global__ void k_fill_int(int* p, int64_t count, int value) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = value;
+}
+
+__global__ void k_count_active(int B, const int* active, int* num_active) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += blockDim.x)
+    if (active[b]) atomicAdd(&cnt, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) *num_active = cnt;
+}
+
+}  // namespace
+
+void launch_fill_int(int* p, int64_t count, int value, cudaStream_t s) {
+  int blocks = (int)std::min<int64_t>((count + 255) / 256, 1024);
+  if (blocks < 1) blocks = 1;
+  qm_note_launch();
+  k_fill_int<<<blocks, 256, 0, s>>>(p, count, value);
+}
+
+void launch_count_active(int B, const int* active, int* num_active, cudaStream_t s) {
+  qm_note_launch();
+  k_count_active<<<1, 256, 0, s>>>(B, active, num_active);
+}
+
+extern "C" {
+
+int qmprs_version(void) { return 100; }
+
+int64_t qmprs_launch_count(void) { return (int64_t)g_launches.load(); }
+
+int qmprs_plan_set_profiling(qmprs_plan_t p, int enable) {
+  if (!p) return QMPRS_ERR_INVALID;
+  p->prof = enable != 0;
+  for (int k = 0; k < 4; ++k) {
+    p->prof_launches[k] = 0;
+    p->prof_ms[k] = 0.0;
+    p->prof_bytes[k] = 0.0;
+  }
+  return QMPRS_OK;
+}
+
+int qmprs_plan_profile(qmprs_plan_t p, int kernel, int64_t* launches, double* milliseconds, double* bytes) {
+  if (!p || kernel < 0 || kernel > 3) return QMPRS_ERR_INVALID;
+  if (launches) *launches = p->prof_launches[kernel];
+  if (milliseconds) *milliseconds = p->prof_ms[kernel];
+  if (bytes) *bytes = p->prof_bytes[kernel];
+  return QMPRS_OK;
+}
+
+int qmprs_create(qmprs_handle_t* out) {
+  if (!out) return QMPRS_ERR_INVALID;
+  qmprs_ctx* h = new qmprs_ctx();
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    *out = nullptr;
+    return QMPRS_ERR_CUDA;
+  }
+  *out = h;
+  return QMPRS_OK;
+}
+
+void qmprs_destroy(qmprs_handle_t h) { delete h; }
+
+const char* qmprs_last_error(qmprs_handle_t h) { return h ? h->err.c_str() : "null handle"; }
+
+void qmprs_plan_destroy(qmprs_plan_t p) {
+  if (!p) return;
+  void* ptrs[] = {p->d_n,      p->d_tile_state, p->d_tile_idx, p->d_state_tile0, p->d_state_ntiles,
+                  p->d_ticket, p->d_err,        p->d_vec_off,  p->d_gate_off,    p->d_tensor_off,
+                  p->d_bond_init, p->S0,        p->S1,         p->S2,            p->partials,
+                  p->tt_partials, p->gram,      p->vsel,       p->vsel2,         p->site_t, p->vwork,
+                  p->bonds,    p->active,       p->nlayers,    p->num_active,    p->nuc,
+                  p->sq,       p->tnorm};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete p;
+}
+
+int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, int max_layers, int max_bond,
+                      qmprs_plan_t* out) {
+  if (!h || !out) return QMPRS_ERR_INVALID;
+  *out = nullptr;
+  if (num_states < 1 || !num_qubits) return set_err(h, QMPRS_ERR_INVALID, "num_states must be >= 1");
+  if (max_layers < 1) return set_err(h, QMPRS_ERR_INVALID, "The number of layers must be a positive integer.");
+  if (max_bond < 1) return set_err(h, QMPRS_ERR_INVALID, "`bond_dimension` must be an integer greater than 0.");
+  qmprs_plan* p = new qmprs_plan();
+  p->h = h;
+  p->B = num_states;
+  p->max_layers = max_layers;
+  p->max_bond = max_bond;
+  p->n.assign(num_qubits, num_qubits + num_states);
+  std::vector<int> tile_state, tile_idx, state_tile0(num_states), state_ntiles(num_states);
+  // Tile size: aim at ~16 tiles per SM over the whole batch (152 SMs), so
+  // that per-tile reduction overhead amortises over many amplitudes; never
+  // below 2^TILE_BITS_MIN amplitudes nor above 2^TILE_BITS_MAX.
+  int64_t total_amps = 0;
+  for (int b = 0; b < num_states; ++b) {
+    const int n = p->n[b];
+    if (n < 2 || n > MAX_QUBITS) {
+      delete p;
+      return set_err(h, QMPRS_ERR_INVALID, "The statevector must have at least 2 qubits (and at most 30).");
+    }
+    total_amps += ipow2(n);
+  }
+  int tile_bits = TILE_BITS_MIN;
+  while (tile_bits < TILE_BITS_MAX && (total_amps >> (tile_bits + 1)) >= 152 * 16) ++tile_bits;
+  p->tile_bits = tile_bits;
+  for (int b = 0; b < num_states; ++b) {
+    const int n = p->n[b];
+    p->max_n = std::max(p->max_n, n);
+    p->vec_off.push_back(p->vec_total);
+    p->vec_total += ipow2(n);
+    p->gate_off.push_back(p->gate_total);
+    p->gate_total += (int64_t)max_layers * n * 16;
+    p->tensor_off.push_back(p->tensor_total);
+    const int ce = chi_eff_host(max_bond, n);
+    p->tensor_total += (int64_t)n * 2 * ce * ce;
+    const int nt = n > tile_bits ? (1 << (n - tile_bits)) : 1;
+    state_tile0[b] = (int)tile_state.size();
+    state_ntiles[b] = nt;
+    for (int t = 0; t < nt; ++t) {
+      tile_state.push_back(b);
+      tile_idx.push_back(t);
+    }
+  }
+  p->ntiles = (int)tile_state.size();
+  std::vector<int> bond_init((size_t)num_states * (p->max_n + 1), 0);
+  for (int b = 0; b < num_states; ++b) {
+    bond_init[(size_t)b * (p->max_n + 1)] = 1;
+    bond_init[(size_t)b * (p->max_n + 1) + p->n[b]] = 1;
+  }
+#define PC(call)                                  \
+  do {                                            \
+    cudaError_t _e = (call);                      \
+    if (_e != cudaSuccess) {                      \
+      int code = cuda_fail(h, _e, #call);         \
+      qmprs_plan_destroy(p);                      \
+      return code;                                \
+    }                                             \
+  } while (0)
+  const int B = num_states;
+  PC(dalloc(&p->d_n, B));
+  PC(dalloc(&p->d_vec_off, B));
+  PC(dalloc(&p->d_gate_off, B));
+  PC(dalloc(&p->d_tensor_off, B));
+  PC(dalloc(&p->d_tile_state, p->ntiles));
+  PC(dalloc(&p->d_tile_idx, p->ntiles));
+  PC(dalloc(&p->d_state_tile0, B));
+  PC(dalloc(&p->d_state_ntiles, B));
+  PC(dalloc(&p->d_ticket, B));
+  PC(dalloc(&p->d_err, 1));
+  PC(dalloc(&p->d_bond_init, (int64_t)bond_init.size()));
+  PC(cudaMemcpy(p->d_n, p->n.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_vec_off, p->vec_off.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_gate_off, p->gate_off.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_tensor_off, p->tensor_off.data(), sizeof(int64_t) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_tile_state, tile_state.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_tile_idx, tile_idx.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_state_tile0, state_tile0.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_state_ntiles, state_ntiles.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_bond_init, bond_init.data(), sizeof(int) * bond_init.size(), cudaMemcpyHostToDevice));
+  PC(cudaMemset(p->d_ticket, 0, sizeof(int) * B));
+  PC(cudaMemset(p->d_err, 0, sizeof(int)));
+  PC(dalloc(&p->S0, p->vec_total));
+  PC(dalloc(&p->S1, p->vec_total));
+  PC(dalloc(&p->S2, p->vec_total));
+  PC(dalloc(&p->partials, (int64_t)p->ntiles * WARPS_PER_BLOCK * 16));
+  PC(dalloc(&p->vsel, (int64_t)B * 16));
+  PC(dalloc(&p->site_t, (int64_t)B * p->max_n * 8));
+  PC(dalloc(&p->bonds, (int64_t)bond_init.size()));
+  PC(dalloc(&p->active, B));
+  PC(dalloc(&p->nlayers, B));
+  PC(dalloc(&p->num_active, 1));
+  PC(dalloc(&p->nuc, B));
+  PC(dalloc(&p->sq, B));
+  PC(dalloc(&p->tnorm, B));
+#undef PC
+  BatchDev& bd = p->bd;
+  bd.B = B;
+  bd.ntiles = p->ntiles;
+  bd.max_n = p->max_n;
+  bd.n = p->d_n;
+  bd.vec_off = p->d_vec_off;
+  bd.gate_off = p->d_gate_off;
+  bd.tensor_off = p->d_tensor_off;
+  bd.tile_state = p->d_tile_state;
+  bd.tile_idx = p->d_tile_idx;
+  bd.state_tile0 = p->d_state_tile0;
+  bd.state_ntiles = p->d_state_ntiles;
+  bd.ticket = p->d_ticket;
+  bd.err = p->d_err;
+  *out = p;
+  return QMPRS_OK;
+}
+
+int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, int64_t* tensor_elems,
+                      int64_t* vec_off, int64_t* gate_off, int64_t* tensor_off) {
+  if (!p) return QMPRS_ERR_INVALID;
+  if (vec_elems) *vec_elems = p->vec_total;
+  if (gate_elems) *gate_elems = p->gate_total;
+  if (tensor_elems) *tensor_elems = p->tensor_total;
+  for (int b = 0; b < p->B; ++b) {
+    if (vec_off) vec_off[b] = p->vec_off[b];
+    if (gate_off) gate_off[b] = p->gate_off[b];
+    if (tensor_off) tensor_off[b] = p->tensor_off[b];
+  }
+  return QMPRS_OK;
+}
+
+int qmprs_plan_max_qubits(qmprs_plan_t p) { return p ? p->max_n : -1; }
+
+int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, double cutoff, void* tensors_,
+                               int* bonds, void* target_, void* stream) {
+  if (!p || !sv_ || !tensors_ || !bonds || !target_) return QMPRS_ERR_INVALID;
+  if (max_bond < 1 || max_bond > p->max_bond)
+    return set_err(p->h, QMPRS_ERR_INVALID, "`bond_dimension` must be an integer in [1, plan max_bond].");
+  if (!(cutoff >= 0.0)) return set_err(p->h, QMPRS_ERR_INVALID, "cutoff must be >= 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float2* sv = (const float2*)sv_;
+  float2* target = (float2*)target_;
+  double2* tensors = (double2*)tensors_;
+  for (int b = 0; b < p->B; ++b)
+    if (chi_eff_host(max_bond, p->n[b]) > TT_MAXB)
+      return set_err(p->h, QMPRS_ERR_UNSUPPORTED,
+                     "statevector -> MPS supports bond dimensions up to 64 (min(bond_dimension, 2^(n/2)) > 64)");
+  const int WW = TT_MAXW * TT_MAXW;
+  if (!p->tt_partials) {
+    CK(dalloc(&p->tt_partials, (int64_t)p->B * TT_SPLIT * WW));
+    CK(dalloc(&p->gram, (int64_t)p->B * WW));
+    CK(dalloc(&p->vsel2, (int64_t)p->B * WW));
+    CK(dalloc(&p->vwork, (int64_t)p->B * WW));
+  }
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  const int64_t nb = (int64_t)p->B * (p->max_n + 1);
+  CK(cudaMemcpyAsync(bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
+  launch_overlap(p->bd, sv, sv, p->partials, p->sq, s);
+  float2* buf[2] = {p->S0, p->S1};
+  for (int j = 0; j + 2 <= p->max_n; ++j) {
+    const float2* src = j == 0 ? sv : buf[(j - 1) & 1];
+    launch_tt_gram(p->bd, j, sv, src, bonds, p->tt_partials, p->gram, s);
+    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond, s);
+    launch_tt_project(p->bd, j, sv, src, buf[j & 1], bonds, p->vsel2, s);
+  }
+  launch_tt_site0(p->bd, buf[0], buf[1], bonds, tensors, p->max_bond, p->sq, s);
+  for (int j = 0; j + 2 <= p->max_n; ++j) {
+    const float2* src = j == 0 ? buf[0] : buf[(j - 1) & 1];
+    launch_mps_contract(p->bd, j, tensors, bonds, p->max_bond, src, buf[j & 1], target, s);
+  }
+  return check_kernel_errors(p, s);
+}
+
+int qmprs_mps_to_statevector(qmprs_plan_t p, const void* tensors, const int* bonds, void* out, void* stream) {
+  if (!p || !tensors || !bonds || !out) return QMPRS_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  float2* buf[2] = {p->S0, p->S1};
+  for (int j = 0; j + 2 <= p->max_n; ++j) {
+    const float2* src = j == 0 ? buf[0] : buf[(j - 1) & 1];
+    launch_mps_contract(p->bd, j, (const double2*)tensors, bonds, p->max_bond, src, buf[j & 1], (float2*)out, s);
+  }
+  CK(cudaGetLastError());
+  return QMPRS_OK;
+}
+
+int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, double fidelity_threshold,
+                         void* gates_, int8_t* arity, int* layers_out, void* layer_fid_, void* stream) {
+  if (!p || !target_ || !gates_ || !arity || !layers_out || !layer_fid_) return QMPRS_ERR_INVALID;
+  if (num_layers < 1 || num_layers > p->max_layers)
+    return set_err(p->h, QMPRS_ERR_INVALID, "The number of layers must be a positive integer (<= plan max_layers).");
+  if (!(fidelity_threshold >= 0.0 && fidelity_threshold <= 1.0))
+    return set_err(p->h, QMPRS_ERR_INVALID, "The fidelity threshold must be a float between 0 and 1.");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float2* target = (const float2*)target_;
+  double2* gates = (double2*)gates_;
+  signed char* ar = (signed char*)arity;
+  double2* layer_fid = (double2*)layer_fid_;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(layers_out, 0, sizeof(int) * p->B, s));
+  CK(cudaMemsetAsync(layer_fid, 0, sizeof(double2) * (size_t)p->B * num_layers, s));
+  launch_fill_int(p->active, p->B, 1, s);
+  float2* work = p->S0;
+  launch_copy_normalize(p->bd, target, work, p->partials, p->sq, s);
+  float2* buf[2] = {p->S1, p->S2};
+  const double atol = 1.0 - fidelity_threshold;
+  const int64_t nb = (int64_t)p->B * (p->max_n + 1);
+  for (int l = 0; l < num_layers; ++l) {
+    CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
+    for (int j = 0; j + 2 <= p->max_n; ++j) {
+      const float2* src = j == 0 ? work : buf[(j - 1) & 1];
+      launch_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->vsel, p->bonds, p->site_t, p->active, s);
+      launch_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s);
+    }
+    launch_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s);
+    for (int j = 0; j < p->max_n; ++j) {
+      GateSel sel;
+      sel.mode = SEL_INVERSE;
+      sel.step = j;
+      sel.layer = l;
+      sel.adjoint = 1;
+      sel.gates = gates;
+      sel.arity = ar;
+      sel.nlayers = nullptr;
+      sel.active = p->active;
+      launch_apply_gate(p->bd, work, sel, s);
+    }
+    launch_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
+    launch_count_active(p->B, p->active, p->num_active, s);
+    int na = 0;
+    CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (na == 0) break;
+  }
+  return check_kernel_errors(p, s);
+}
+
+int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, const int8_t* arity,
+                          const int* num_layers, int num_sweeps, double stop_fidelity, double* sweep_fid,
+                          int* sweeps_done, void* stream) {
+  if (!p || !target_ || !gates_ || !arity || !num_layers || !sweep_fid || !sweeps_done) return QMPRS_ERR_INVALID;
+  if (num_sweeps < 0) return set_err(p->h, QMPRS_ERR_INVALID, "num_sweeps must be >= 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float2* target = (const float2*)target_;
+  double2* gates = (double2*)gates_;
+  const signed char* ar = (const signed char*)arity;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(sweeps_done, 0, sizeof(int) * p->B, s));
+  if (num_sweeps == 0) return QMPRS_OK;
+  CK(cudaMemsetAsync(sweep_fid, 0, sizeof(double) * (size_t)p->B * num_sweeps, s));
+  int max_gates = 0;
+  int rc = read_max_gates(p, num_layers, s, &max_gates);
+  if (rc != QMPRS_OK) return rc;
+  launch_fill_int(p->active, p->B, 1, s);
+  launch_overlap(p->bd, target, target, p->partials, p->tnorm, s);
+  float2* psi = p->S0;
+  float2* t = p->S1;
+  ProfLog log;
+  const bool prof = p->prof;
+  std::vector<int> act(p->B, 1);
+  for (int sw = 0; sw < num_sweeps; ++sw) {
+    // algorithmic bytes per step j, counted from the states active in this sweep
+    std::vector<double> amp_at(prof ? max_gates : 0, 0.0);
+    if (prof) {
+      CK(cudaMemcpyAsync(act.data(), p->active, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int b = 0; b < p->B; ++b)
+        if (act[b])
+          for (int j = 0; j < p->gates_per_state[b]; ++j) amp_at[j] += (double)ipow2(p->n[b]);
+    }
+    launch_set_zero_state(p->bd, psi, p->active, s);
+    GateSel sel;
+    sel.layer = 0;
+    sel.gates = gates;
+    sel.arity = ar;
+    sel.nlayers = num_layers;
+    sel.active = p->active;
+    sel.mode = SEL_REBUILD;
+    sel.adjoint = 0;
+    for (int j = 0; j < max_gates; ++j) {
+      sel.step = j;
+      log.begin(prof, s);
+      launch_apply_gate(p->bd, psi, sel, s);
+      log.end(prof, 2, s);
+      if (prof) p->prof_bytes[2] += 16.0 * amp_at[j];
+    }
+    CK(cudaMemcpyAsync(t, target, sizeof(float2) * p->vec_total, cudaMemcpyDeviceToDevice, s));
+    sel.mode = SEL_SWEEP;
+    sel.adjoint = 1;
+    for (int j = 0; j < max_gates; ++j) {
+      log.begin(prof, s);
+      launch_sweep_env(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
+      log.end(prof, 0, s);
+      log.begin(prof, s);
+      launch_sweep_polar(p->bd, j, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
+      log.end(prof, 3, s);
+      sel.step = j;
+      log.begin(prof, s);
+      launch_apply_gate(p->bd, t, sel, s);
+      log.end(prof, 1, s);
+      if (prof) {
+        p->prof_bytes[0] += 24.0 * amp_at[j];
+        p->prof_bytes[1] += 16.0 * amp_at[j];
+      }
+    }
+    log.flush(p);
+    CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));
+    launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active, stop_fidelity,
+                        p->num_active, s);
+    if (stop_fidelity > 0.0) {
+      int na = 0;
+      CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (na == 0) break;
+    }
+  }
+  return check_kernel_errors(p, s);
+}
+
+int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, const int* num_layers, void* out,
+                        void* stream) {
+  if (!p || !gates || !arity || !num_layers || !out) return QMPRS_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  int max_gates = 0;
+  int rc = read_max_gates(p, num_layers, s, &max_gates);
+  if (rc != QMPRS_OK) return rc;
+  float2* psi = (float2*)out;
+  launch_set_zero_state(p->bd, psi, nullptr, s);
+  GateSel sel;
+  sel.mode = SEL_REBUILD;
+  sel.layer = 0;
+  sel.adjoint = 0;
+  sel.gates = (const double2*)gates;
+  sel.arity = (const signed char*)arity;
+  sel.nlayers = num_layers;
+  sel.active = nullptr;
+  for (int j = 0; j < max_gates; ++j) {
+    sel.step = j;
+    launch_apply_gate(p->bd, psi, sel, s);
+  }
+  CK(cudaGetLastError());
+  return QMPRS_OK;
+}
+
+int qmprs_overlap(qmprs_plan_t p, const void* a, const void* b, void* out, void* stream) {
+  if (!p || !a || !b || !out) return QMPRS_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  launch_overlap(p->bd, (const float2*)a, (const float2*)b, p->partials, (double2*)out, s);
+  CK(cudaGetLastError());
+  return QMPRS_OK;
+}
+
+int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t* arity, int layer, int inverse,
+                      void* stream) {
+  if (!p || !vec || !gates || !arity) return QMPRS_ERR_INVALID;
+  if (layer < 0 || layer >= p->max_layers) return set_err(p->h, QMPRS_ERR_INVALID, "layer index out of range");
+  cudaStream_t s = (cudaStream_t)stream;
+  GateSel sel;
+  sel.mode = inverse ? SEL_INVERSE : SEL_LAYER_FWD;
+  sel.layer = layer;
+  sel.adjoint = inverse ? 1 : 0;
+  sel.gates = (const double2*)gates;
+  sel.arity = (const signed char*)arity;
+  sel.nlayers = nullptr;
+  sel.active = nullptr;
+  for (int j = 0; j < p->max_n; ++j) {
+    sel.step = j;
+    launch_apply_gate(p->bd, (float2*)vec, sel, s);
+  }
+  CK(cudaGetLastError());
+  return QMPRS_OK;
+}
+
+}  // extern "C"

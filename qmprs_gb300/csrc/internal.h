@@ -1,0 +1,146 @@
+// Internal declarations of the qmprs_gb300 CUDA library.
+//
+// Layout in HBM (all caller buffers are contiguous):
+//   vectors  complex64, state b occupies [vec_off[b], vec_off[b] + 2^n_b);
+//            amplitude index bit (n-1-q) is qubit q (MSB order, the
+//            reference's convention).
+//   gates    complex128, state b, generated layer l, site s at
+//            gate_off[b] + (l * n_b + s) * 16; a two-qubit gate is a
+//            row-major 4x4 (rows = outputs), a one-qubit gate uses the first
+//            four entries as a row-major 2x2.  Layers are stored in the order
+//            they are generated; the circuit applies them in reverse.
+//   arity    int8, same indexing as gates without the factor 16 (1 or 2).
+//   tensors  complex128 MPS site tensors (l, p, r), site s of state b at
+//            tensor_off[b] + s * 2 * chi * chi.
+//   bonds    int32, state b at b * (max_n + 1): bonds[c] is the bond between
+//            sites c-1 and c, bonds[0] = bonds[n] = 1.
+//
+// Work decomposition: every state is cut into tiles of 2^tile_bits
+// amplitudes (one tile if the state is smaller); the plan picks tile_bits in
+// [TILE_BITS_MIN, TILE_BITS_MAX] so that the batch has about 16 tiles per SM.
+// A launch runs a grid-stride loop over the tiles of all states of the
+// batch, so states of uneven size share one launch.  Per-state reductions
+// write one fp64 partial per warp of each tile; a second kernel (one block
+// or warp per state) sums them in a fixed order, which keeps every result
+// deterministic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qm_complex.h"
+
+#define TILE_BITS_MIN 12
+#define TILE_BITS_MAX 17
+#define WARPS_PER_BLOCK 8   // BLOCK_THREADS / 32; per-warp partials per tile
+#define BLOCK_THREADS 256
+#define MAX_QUBITS 30
+#define TT_MAXW 128   // widest Gram of stage (a): 2 * bond
+#define TT_MAXB 64    // largest MPS bond of stage (a)
+
+enum {
+  QM_OK = 0,
+  QM_ERR_INVALID = 1,
+  QM_ERR_UNSUPPORTED = 2,
+  QM_ERR_CUDA = 3,
+  QM_ERR_NUMERIC = 4,
+  QM_ERR_NONUNITARY = 5,
+};
+
+// error flags raised by kernels (bit mask in dev_err)
+enum {
+  KERR_NONUNITARY = 1,
+  KERR_EIG_WIDTH = 2,
+  KERR_NONFINITE = 4,
+  KERR_BAD_GATE = 8,
+};
+
+struct BatchDev {
+  int B;
+  int ntiles;
+  int max_n;
+  const int* n;            // [B] qubits
+  const int64_t* vec_off;  // [B]
+  const int64_t* gate_off; // [B]
+  const int64_t* tensor_off;  // [B]
+  const int* tile_state;   // [ntiles]
+  const int* tile_idx;     // [ntiles] tile index within its state
+  const int* state_tile0;  // [B]
+  const int* state_ntiles; // [B]
+  int* ticket;             // [B] last-tile tickets (kept at zero between launches)
+  int* err;                // [1] error flag bits
+};
+
+// Gate selection modes for the per-step gate launches.
+enum {
+  SEL_REBUILD = 0,   // forward circuit order, gate j of C (circuit state)
+  SEL_SWEEP = 1,     // backward circuit order, gate j from the end
+  SEL_INVERSE = 2,   // adjoint of generated layer `layer`, sites n-1 .. 0
+  SEL_LAYER_FWD = 3, // generated layer `layer` itself, sites 0 .. n-1
+};
+
+struct GateSel {
+  int mode;
+  int step;             // j
+  int layer;            // for SEL_INVERSE
+  int adjoint;          // apply G^H instead of G
+  const double2* gates;
+  const signed char* arity;
+  const int* nlayers;   // [B] generated layers per state
+  const int* active;    // [B] state participates (may be null)
+};
+
+// ---- launches (defined in the .cu files) ---------------------------------
+void launch_set_zero_state(const BatchDev& bd, float2* vec, const int* active, cudaStream_t s);
+void launch_apply_gate(const BatchDev& bd, float2* vec, const GateSel& sel, cudaStream_t s);
+void launch_overlap(const BatchDev& bd, const float2* a, const float2* b, double2* partials,
+                    double2* out, cudaStream_t s);
+void launch_copy_normalize(const BatchDev& bd, const float2* src, float2* dst, double2* partials,
+                           double2* sq_norms, cudaStream_t s);
+
+// (b) layer generation
+void launch_layer_gram(const BatchDev& bd, int step, const float2* work, const float2* src,
+                       const int* bonds, double2* partials, double2* vsel, int* bonds_out,
+                       double2* site_t, const int* active, cudaStream_t s);
+void launch_layer_project(const BatchDev& bd, int step, const float2* work, const float2* src,
+                          float2* dst, const int* bonds, const double2* vsel, const int* active,
+                          cudaStream_t s);
+void launch_layer_build(const BatchDev& bd, int layer, const float2* rem0, const float2* rem1,
+                        const int* bonds, double2* site_t, double2* gates, signed char* arity,
+                        const int* active, cudaStream_t s);
+void launch_layer_fidelity(const BatchDev& bd, int layer, const float2* work, int num_layers,
+                           double atol, double2* layer_fid, int* nlayers, int* active,
+                           cudaStream_t s);
+
+// (d) sweep
+void launch_sweep_env(const BatchDev& bd, int step, float2* psi, const float2* t,
+                      double2* gates, const signed char* arity, const int* nlayers,
+                      const int* active, double2* partials, double* nuc, cudaStream_t s);
+void launch_sweep_polar(const BatchDev& bd, int step, double2* gates, const signed char* arity,
+                        const int* nlayers, const int* active, const double2* partials, double* nuc,
+                        cudaStream_t s);
+void launch_sweep_finish(int B, int sweep, int num_sweeps, const double* nuc, const double2* tnorm2,
+                         double* sweep_fid, int* sweeps_done, int* active, double stop_fid,
+                         int* num_active, cudaStream_t s);
+
+// (a) statevector -> MPS
+void launch_tt_gram(const BatchDev& bd, int step, const float2* sv, const float2* src, const int* bonds,
+                    double2* partials, double2* gram, cudaStream_t s);
+void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, double2* vwork, int max_bond,
+                   double cutoff, double2* vsel, double2* tensors, int chi, cudaStream_t s);
+void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const float2* src, float2* dst,
+                       const int* bonds, const double2* vsel, cudaStream_t s);
+void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1, const int* bonds,
+                     double2* tensors, int chi, const double2* in_sq, cudaStream_t s);
+void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,
+                         const float2* src, float2* dst_buf, float2* target, cudaStream_t s);
+
+// misc
+void qm_note_launch();   // counts every kernel launch the library issues
+void launch_fill_int(int* p, int64_t count, int value, cudaStream_t s);
+void launch_count_active(int B, const int* active, int* num_active, cudaStream_t s);
+
+#define TT_SPLIT 8
+
+// helpers
+__host__ __device__ inline int64_t ipow2(int k) { return (int64_t)1 << k; }

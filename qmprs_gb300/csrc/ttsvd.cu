@@ -1,0 +1,379 @@
+// (a) statevector -> MPS: right-to-left sequential truncated SVD to bond chi.
+//
+// Restates MPS.from_statevector (reference qmprs/primitives/mps.py:219-249):
+// quimb's from_dense followed by tensor_network_1d_compress(max_bond=chi),
+// whose density-matrix method truncates from the right and leaves a
+// right-canonical MPS.  Cut c (c = n-1 .. 1) of state b holds the remainder
+// M (2^c x w, w = 2 r, r = bond c+1).  Per cut:
+//   k_tt_gram     Gram matrix M^H M in fp64, split over at most TT_SPLIT
+//                 row ranges per state, partials reduced in order;
+//   k_tt_eig      one CTA per state: parallel cyclic Jacobi (round-robin
+//                 pairs) on the w x w Gram, fp64, working set in global
+//                 memory (L2 resident); sort, rsum2 cutoff + max_bond,
+//                 canonical phases; site tensor c;
+//   k_tt_project  next remainder M V (fp32).
+// k_tt_site0 stores site 0 (the last remainder, rescaled to the input norm,
+// as quimb's rsum2 renormalisation does) and k_mps_contract rebuilds the
+// truncated dense target, left to right.
+//
+// Supported widths: w <= TT_MAXW (bonds <= TT_MAXB).  A state whose Gram
+// would be wider raises KERR_EIG_WIDTH and has its bond poisoned (-1); every
+// later kernel of the stage skips a state whose bonds are out of range, so
+// no access ever depends on an unset bond.
+#include "device_common.cuh"
+
+#define TT_CH 32
+
+__host__ __device__ inline int chi_eff(int chi, int n) {
+  const int cap = 1 << (n / 2);
+  return chi < cap ? chi : cap;
+}
+
+__device__ __forceinline__ bool bond_ok(int r) { return r >= 1 && r <= TT_MAXB; }
+
+__global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step, const float2* sv,
+                                                           const float2* src, const int* bonds,
+                                                           double2* partials, double2* gram) {
+  __shared__ float2 xs[TT_CH][TT_MAXW];
+  const int WW = TT_MAXW * TT_MAXW;
+  for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
+    const int b = bd.tile_state[tile];
+    const int n = bd.n[b];
+    const int c = n - 1 - step;
+    if (c < 1) continue;
+    const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
+    const int r = bond[c + 1];
+    const int idx = bd.tile_idx[tile];
+    if (!bond_ok(r)) {
+      if (r > TT_MAXB && idx == 0 && threadIdx.x == 0) atomicOr(bd.err, KERR_EIG_WIDTH);
+      continue;
+    }
+    const int w = 2 * r;
+    const int nt = bd.state_ntiles[b];
+    const int nsplit = nt < TT_SPLIT ? nt : TT_SPLIT;
+    if (idx >= nsplit) continue;
+    const float2* m = (step == 0 ? sv : src) + bd.vec_off[b];
+    int64_t lo, hi;
+    tile_range(ipow2(c), idx, nsplit, &lo, &hi);
+    double2* part = partials + ((int64_t)b * TT_SPLIT + idx) * WW;
+    for (int e0 = 0; e0 < w * w; e0 += 16 * BLOCK_THREADS) {
+      double2 acc[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) acc[i] = czero();
+      for (int64_t r0 = lo; r0 < hi; r0 += TT_CH) {
+        const int nr = (int)((hi - r0) < TT_CH ? (hi - r0) : TT_CH);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nr * w; e += blockDim.x) xs[e / w][e % w] = m[(r0 + e / w) * w + e % w];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int e = e0 + threadIdx.x + i * BLOCK_THREADS;
+          if (e < w * w) {
+            const int a = e / w, cc = e % w;
+            double2 s = acc[i];
+            for (int rr = 0; rr < nr; ++rr) {
+              const double2 x = f2d(xs[rr][a]), y = f2d(xs[rr][cc]);
+              s.x += x.x * y.x + x.y * y.y;
+              s.y += x.x * y.y - x.y * y.x;
+            }
+            acc[i] = s;
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int e = e0 + threadIdx.x + i * BLOCK_THREADS;
+        if (e < w * w) part[e] = acc[i];
+      }
+    }
+    __syncthreads();
+    if (last_tile_ticket(bd.ticket, b, nsplit)) {
+      for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+        double2 s = czero();
+        for (int t = 0; t < nsplit; ++t) s = cadd(s, ld_cg(&partials[((int64_t)b * TT_SPLIT + t) * WW + e]));
+        gram[(int64_t)b * WW + e] = s;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) bd.ticket[b] = 0;
+    }
+  }
+}
+
+// One CTA per state; G (in place in `gram`) and V (`vwork`) are row-major
+// w x w in global memory.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step, int* bonds, double2* gram,
+                                                          double2* vwork, int max_bond, double cutoff,
+                                                          double2* vsel, double2* tensors, int chi) {
+  __shared__ double s_c[TT_MAXW / 2];
+  __shared__ double2 s_se[TT_MAXW / 2], s_sce[TT_MAXW / 2];
+  __shared__ int s_p[TT_MAXW / 2], s_q[TT_MAXW / 2], s_flag[TT_MAXW / 2];
+  __shared__ int s_rot;
+  __shared__ double s_lam[TT_MAXW];
+  __shared__ int s_perm[TT_MAXW];
+  __shared__ int s_keep;
+  const int WW = TT_MAXW * TT_MAXW;
+  const int b = blockIdx.x;
+  if (b >= bd.B) return;
+  const int n = bd.n[b];
+  const int c = n - 1 - step;
+  if (c < 1) return;
+  int* bond = bonds + (int64_t)b * (bd.max_n + 1);
+  const int r = bond[c + 1];
+  if (!bond_ok(r)) {
+    if (threadIdx.x == 0) bond[c] = -1;   // poison: every later step skips this state
+    return;
+  }
+  const int w = 2 * r;
+  double2* G = gram + (int64_t)b * WW;
+  double2* V = vwork + (int64_t)b * WW;
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[e] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
+  __syncthreads();
+  const int half = w / 2;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int k = 0; k < w - 1; ++k) {
+      if (threadIdx.x < half) {
+        const int i = threadIdx.x;
+        const int t1 = i, t2 = w - 1 - i;
+        int p = t1 == 0 ? 0 : 1 + ((t1 - 1 + k) % (w - 1));
+        int q = 1 + ((t2 - 1 + k) % (w - 1));
+        if (p > q) { const int tmp = p; p = q; q = tmp; }
+        const double2 g = G[p * w + q];
+        const double ag = cabs_(g);
+        const double app = G[p * w + p].x, aqq = G[q * w + q].x;
+        const int rot = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)));
+        s_p[i] = p;
+        s_q[i] = q;
+        s_flag[i] = rot;
+        if (rot) {
+          const double zeta = (aqq - app) / (2.0 * ag);
+          const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double cc = 1.0 / sqrt(1.0 + t * t);
+          const double ss = cc * t;
+          const double2 e = cscale(g, 1.0 / ag);
+          s_c[i] = cc;
+          s_se[i] = cscale(e, ss);
+          s_sce[i] = cscale(cconj(e), ss);
+          s_rot = 1;
+        }
+      }
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
+        const int i = idx / w, row = idx % w;
+        if (!s_flag[i]) continue;
+        const int p = s_p[i], q = s_q[i];
+        const double cc = s_c[i];
+        const double2 se = s_se[i], sce = s_sce[i];
+        const double2 xp = G[row * w + p], xq = G[row * w + q];
+        G[row * w + p] = csub(cscale(xp, cc), cmul(sce, xq));
+        G[row * w + q] = cadd(cmul(se, xp), cscale(xq, cc));
+        const double2 vp = V[row * w + p], vq = V[row * w + q];
+        V[row * w + p] = csub(cscale(vp, cc), cmul(sce, vq));
+        V[row * w + q] = cadd(cmul(se, vp), cscale(vq, cc));
+      }
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
+        const int i = idx / w, col = idx % w;
+        if (!s_flag[i]) continue;
+        const int p = s_p[i], q = s_q[i];
+        const double cc = s_c[i];
+        const double2 se = s_se[i], sce = s_sce[i];
+        const double2 xp = G[p * w + col], xq = G[q * w + col];
+        G[p * w + col] = csub(cscale(xp, cc), cmul(se, xq));
+        G[q * w + col] = cadd(cmul(sce, xp), cscale(xq, cc));
+      }
+      __syncthreads();
+      if (threadIdx.x < half && s_flag[threadIdx.x]) {
+        const int p = s_p[threadIdx.x], q = s_q[threadIdx.x];
+        G[p * w + q] = czero();
+        G[q * w + p] = czero();
+        G[p * w + p].y = 0.0;
+        G[q * w + q].y = 0.0;
+      }
+      __syncthreads();
+    }
+    if (!s_rot) break;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * w + i].x; }
+    for (int i = 1; i < w; ++i) {
+      const int kk = s_perm[i];
+      const double key = s_lam[i];
+      int j = i - 1;
+      while (j >= 0 && s_lam[j] < key) { s_lam[j + 1] = s_lam[j]; s_perm[j + 1] = s_perm[j]; --j; }
+      s_lam[j + 1] = key;
+      s_perm[j + 1] = kk;
+    }
+    int keep = rank_by_cutoff(s_lam, w, cutoff, max_bond);
+    if (keep > TT_MAXB) keep = TT_MAXB;
+    if (c < 30 && keep > (1 << c)) keep = 1 << c;   // M has 2^c rows: rank <= 2^c
+    s_keep = keep;
+    bond[c] = keep;
+  }
+  __syncthreads();
+  const int keep = s_keep;
+  if (threadIdx.x < keep) phase_fix_column(V, w, w, s_perm[threadIdx.x]);
+  __syncthreads();
+  double2* vs = vsel + (int64_t)b * WW;
+  for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
+    const int a = e / keep, col = e % keep;
+    vs[a * TT_MAXB + col] = V[a * w + s_perm[col]];
+  }
+  const int ce = chi_eff(chi, n);
+  double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
+  for (int e = threadIdx.x; e < keep * 2 * r; e += blockDim.x) {
+    const int l = e / (2 * r), pr = e % (2 * r);   // e = l * 2r + (p * r + rr)
+    ts[e] = cconj(V[pr * w + s_perm[l]]);
+  }
+}
+
+// Dynamic shared memory: V (TT_MAXW x TT_MAXB float2) then TT_CH rows.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_tt_project(BatchDev bd, int step, const float2* sv,
+                                                              const float2* src, float2* dst,
+                                                              const int* bonds, const double2* vsel) {
+  extern __shared__ float2 sh[];
+  float2* vs = sh;
+  float2* xs = sh + TT_MAXW * TT_MAXB;
+  const int WW = TT_MAXW * TT_MAXW;
+  for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
+    const int b = bd.tile_state[tile];
+    const int n = bd.n[b];
+    const int c = n - 1 - step;
+    if (c < 1) continue;
+    const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
+    const int r = bond[c + 1];
+    const int keep = bond[c];
+    if (!bond_ok(r) || !bond_ok(keep)) continue;
+    const int w = 2 * r;
+    __syncthreads();
+    for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
+      const double2 v = vsel[(int64_t)b * WW + (e / keep) * TT_MAXB + (e % keep)];
+      vs[e] = cf((float)v.x, (float)v.y);
+    }
+    const float2* m = (step == 0 ? sv : src) + bd.vec_off[b];
+    float2* o = dst + bd.vec_off[b];
+    int64_t lo, hi;
+    tile_range(ipow2(c), bd.tile_idx[tile], bd.state_ntiles[b], &lo, &hi);
+    for (int64_t r0 = lo; r0 < hi; r0 += TT_CH) {
+      const int nr = (int)((hi - r0) < TT_CH ? (hi - r0) : TT_CH);
+      __syncthreads();
+      for (int e = threadIdx.x; e < nr * w; e += blockDim.x) xs[(e / w) * TT_MAXW + e % w] = m[(r0 + e / w) * w + e % w];
+      __syncthreads();
+      for (int e = threadIdx.x; e < nr * keep; e += blockDim.x) {
+        const int rr = e / keep, col = e % keep;
+        float2 acc = cf(0.f, 0.f);
+        for (int a = 0; a < w; ++a) acc = fmac(acc, xs[rr * TT_MAXW + a], vs[a * keep + col]);
+        o[(r0 + rr) * keep + col] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_tt_site0(BatchDev bd, const float2* rem0, const float2* rem1, const int* bonds,
+                           double2* tensors, int chi, const double2* in_sq) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bd.B; b += gridDim.x * blockDim.x) {
+    const int n = bd.n[b];
+    const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
+    const int r1 = bond[1];
+    if (!bond_ok(r1)) continue;
+    const float2* rem = (((n - 2) & 1) ? rem1 : rem0) + bd.vec_off[b];
+    double nrm = 0.0;
+    for (int i = 0; i < 2 * r1; ++i) nrm += cnorm2(f2d(rem[i]));
+    nrm = sqrt(nrm);
+    const double f = nrm > 0.0 ? sqrt(in_sq[b].x) / nrm : 0.0;
+    double2* ts = tensors + bd.tensor_off[b];
+    for (int i = 0; i < 2 * r1; ++i) ts[i] = cscale(f2d(rem[i]), f);
+  }
+}
+
+// v_{c+1}[(x, p), r'] = sum_r v_c[x, r] A_c[r, p, r'], c = step + 1.
+// Dynamic shared memory: A_c as float2, at most TT_MAXB x 2 x TT_MAXB.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_mps_contract(BatchDev bd, int step, const double2* tensors,
+                                                                const int* bonds, int chi,
+                                                                const float2* src, float2* dst_buf,
+                                                                float2* target) {
+  extern __shared__ float2 as[];
+  for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
+    const int b = bd.tile_state[tile];
+    const int n = bd.n[b];
+    const int c = step + 1;
+    if (c > n - 1) continue;
+    const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
+    const int rc = bond[c], rn = bond[c + 1];
+    if (!bond_ok(rc) || !bond_ok(rn)) continue;
+    const int ce = chi_eff(chi, n);
+    const double2* a = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
+    __syncthreads();
+    for (int e = threadIdx.x; e < rc * 2 * rn; e += blockDim.x) as[e] = cf((float)a[e].x, (float)a[e].y);
+    __syncthreads();
+    const double2* t0 = tensors + bd.tensor_off[b];
+    const float2* s = src + bd.vec_off[b];
+    float2* o = (c == n - 1 ? target : dst_buf) + bd.vec_off[b];
+    const int64_t total = ipow2(c + 1) * rn;
+    int64_t lo, hi;
+    tile_range(total, bd.tile_idx[tile], bd.state_ntiles[b], &lo, &hi);
+    for (int64_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+      const int64_t x = e / (2 * rn);
+      const int pr = (int)(e % (2 * rn));
+      float2 acc = cf(0.f, 0.f);
+      for (int rr = 0; rr < rc; ++rr) {
+        float2 sv;
+        if (step == 0) { const double2 d = t0[x * rc + rr]; sv = cf((float)d.x, (float)d.y); }
+        else sv = s[x * rc + rr];
+        acc = fmac(acc, sv, as[rr * 2 * rn + pr]);
+      }
+      o[e] = acc;
+    }
+  }
+}
+
+static int grid_for(const BatchDev& bd) {
+  int g = bd.ntiles;
+  const int cap = 152 * 8;
+  return g < cap ? g : cap;
+}
+
+void launch_tt_gram(const BatchDev& bd, int step, const float2* sv, const float2* src, const int* bonds,
+                    double2* partials, double2* gram, cudaStream_t s) {
+  qm_note_launch();
+  k_tt_gram<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, step, sv, src, bonds, partials, gram);
+}
+
+void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, double2* vwork, int max_bond,
+                   double cutoff, double2* vsel, double2* tensors, int chi, cudaStream_t s) {
+  qm_note_launch();
+  k_tt_eig<<<bd.B, BLOCK_THREADS, 0, s>>>(bd, step, bonds, gram, vwork, max_bond, cutoff, vsel, tensors, chi);
+}
+
+void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const float2* src, float2* dst,
+                       const int* bonds, const double2* vsel, cudaStream_t s) {
+  const size_t smem = sizeof(float2) * (TT_MAXW * TT_MAXB + TT_CH * TT_MAXW);
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_tt_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  qm_note_launch();
+  k_tt_project<<<grid_for(bd), BLOCK_THREADS, smem, s>>>(bd, step, sv, src, dst, bonds, vsel);
+}
+
+void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1, const int* bonds,
+                     double2* tensors, int chi, const double2* in_sq, cudaStream_t s) {
+  qm_note_launch();
+  k_tt_site0<<<(bd.B + 127) / 128, 128, 0, s>>>(bd, rem0, rem1, bonds, tensors, chi, in_sq);
+}
+
+void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,
+                         const float2* src, float2* dst_buf, float2* target, cudaStream_t s) {
+  const size_t smem = sizeof(float2) * TT_MAXB * 2 * TT_MAXB;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_mps_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  qm_note_launch();
+  k_mps_contract<<<grid_for(bd), BLOCK_THREADS, smem, s>>>(bd, step, tensors, bonds, chi, src, dst_buf, target);
+}

@@ -1,0 +1,371 @@
+"""Batched GPU encoding engine (host side of the C ABI).
+
+``Engine.encode`` runs the reference's whole ``prepare_state`` path for a
+batch of statevectors of possibly different qubit counts:
+
+1. ``qmprs_mps_from_statevector``  (a)  ``MPS.from_statevector``
+2. ``qmprs_unitary_layers``        (b)+(c) ``Sequential._get_unitary_layers``
+3. ``qmprs_optimize_layers``       (d)  ``Sequential._optimize_unitary_layers``
+4. ``qmprs_circuit_state`` + ``qmprs_overlap``  fidelity |<sv|C|0>|
+
+PyTorch provides device memory, pinned host memory and the stream; all
+arithmetic runs in the library's kernels.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native
+
+_tls = threading.local()
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class Handle:
+    """One library handle per host thread (handles are not shared)."""
+
+    def __init__(self):
+        if not torch.cuda.is_available():
+            raise RuntimeError("qmprs_gb300 needs a CUDA device (no CPU fallback)")
+        self.lib = _native.load()
+        h = ctypes.c_void_p()
+        code = self.lib.qmprs_create(ctypes.byref(h))
+        if code != 0:
+            raise _native.NativeError(code, "qmprs_create failed")
+        self.h = h
+
+    def check(self, code: int) -> None:
+        _native.raise_for(code, self.h)
+
+    def __del__(self):
+        try:
+            self.lib.qmprs_destroy(self.h)
+        except Exception:
+            pass
+
+
+def handle() -> Handle:
+    h = getattr(_tls, "handle", None)
+    if h is None:
+        h = Handle()
+        _tls.handle = h
+    return h
+
+
+class Plan:
+    """A batch layout: offsets of every state in the caller buffers."""
+
+    def __init__(self, hd: Handle, nqubits: list[int], max_layers: int, max_bond: int):
+        self.hd = hd
+        self.lib = hd.lib
+        self.nqubits = [int(n) for n in nqubits]
+        self.B = len(self.nqubits)
+        self.max_layers = int(max_layers)
+        self.max_bond = int(max_bond)
+        arr = (ctypes.c_int * self.B)(*self.nqubits)
+        p = ctypes.c_void_p()
+        hd.check(self.lib.qmprs_plan_create(hd.h, self.B, arr, self.max_layers, self.max_bond, ctypes.byref(p)))
+        self.p = p
+        ve, ge, te = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        vo = (ctypes.c_int64 * self.B)()
+        go = (ctypes.c_int64 * self.B)()
+        to = (ctypes.c_int64 * self.B)()
+        hd.check(self.lib.qmprs_plan_layout(p, ctypes.byref(ve), ctypes.byref(ge), ctypes.byref(te), vo, go, to))
+        self.vec_elems, self.gate_elems, self.tensor_elems = ve.value, ge.value, te.value
+        self.vec_off = np.array(vo[:], dtype=np.int64)
+        self.gate_off = np.array(go[:], dtype=np.int64)
+        self.tensor_off = np.array(to[:], dtype=np.int64)
+        self.max_n = self.lib.qmprs_plan_max_qubits(p)
+
+    def chi_eff(self, b: int) -> int:
+        return min(self.max_bond, 2 ** (self.nqubits[b] // 2))
+
+    def __del__(self):
+        try:
+            self.lib.qmprs_plan_destroy(self.p)
+        except Exception:
+            pass
+
+
+@dataclass
+class BatchResult:
+    nqubits: list
+    gates: np.ndarray            # complex128 gate store (generation order)
+    arity: np.ndarray            # int8
+    num_layers: np.ndarray       # int32 [B]
+    layer_fidelities: np.ndarray  # complex128 [B, L]
+    sweep_fidelities: np.ndarray  # float64 [B, S]
+    sweeps_done: np.ndarray      # int32 [B]
+    fidelity: np.ndarray         # float64 [B] |<sv|C|0>|
+    gate_off: np.ndarray
+    tensors: np.ndarray | None = None
+    tensor_off: np.ndarray | None = None
+    bonds: np.ndarray | None = None
+    max_n: int = 0
+    max_bond: int = 0
+    timings: dict = field(default_factory=dict)
+
+    def layers(self, b: int) -> list:
+        """Layers of state b in CIRCUIT order, as the reference's ``UnitaryLayer`` lists.
+
+        Each layer is a list of blocks ``(start, end, [gate, ...])``; the
+        gate of the block's last site is 2x2, the others 4x4
+        (``qmprs/primitives/mps.py:46-47``).
+        """
+        n = self.nqubits[b]
+        L = int(self.num_layers[b])
+        base = int(self.gate_off[b])
+        out = []
+        for l in range(L - 1, -1, -1):
+            blocks = []
+            start = 0
+            gates = []
+            for s in range(n):
+                slot = l * n + s
+                k = int(self.arity[base // 16 + slot])
+                raw = self.gates[base + slot * 16: base + slot * 16 + 16]
+                g = raw[:4].reshape(2, 2).copy() if k == 1 else raw.reshape(4, 4).copy()
+                gates.append(g)
+                if k == 1:
+                    blocks.append((start, s, gates))
+                    start = s + 1
+                    gates = []
+            out.append(blocks)
+        return out
+
+    def mps_tensors(self, b: int) -> list:
+        """Site tensors (l, p, r) of state b's MPS from stage (a)."""
+        n = self.nqubits[b]
+        ce = min(self.max_bond, 2 ** (n // 2))
+        bonds = self.bonds[b * (self.max_n + 1): b * (self.max_n + 1) + n + 1]
+        base = int(self.tensor_off[b])
+        out = []
+        for s in range(n):
+            l, r = int(bonds[s]), int(bonds[s + 1])
+            off = base + s * 2 * ce * ce
+            out.append(self.tensors[off: off + l * 2 * r].reshape(l, 2, r).copy())
+        return out
+
+
+class Engine:
+    """Runs the encoding path for batches of states on the current CUDA device."""
+
+    def __init__(self):
+        self.hd = handle()
+        self.lib = self.hd.lib
+        self._plans: dict = {}
+
+    def plan(self, nqubits, max_layers: int, max_bond: int) -> Plan:
+        key = (tuple(int(n) for n in nqubits), int(max_layers), int(max_bond))
+        p = self._plans.get(key)
+        if p is None:
+            p = Plan(self.hd, list(key[0]), key[1], key[2])
+            self._plans[key] = p
+        return p
+
+    @staticmethod
+    def pack(statevectors) -> tuple[list[int], np.ndarray]:
+        """Concatenate complex statevectors (already Ket-normalised) as complex64."""
+        ns, parts = [], []
+        for v in statevectors:
+            v = np.asarray(v).reshape(-1)
+            n = int(round(np.log2(v.size)))
+            if 2 ** n != v.size:
+                raise ValueError("statevector length must be a power of two")
+            ns.append(n)
+            parts.append(v.astype(np.complex64))
+        return ns, np.concatenate(parts)
+
+    # ---- stages --------------------------------------------------------------
+    def upload(self, statevectors, max_layers: int, max_bond: int):
+        """Plan the batch and copy the (Ket-normalised) statevectors to the device."""
+        ns, host = self.pack(statevectors)
+        p = self.plan(ns, max_layers, max_bond)
+        pinned = torch.from_numpy(host.view(np.float32)).pin_memory()
+        sv = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        sv.copy_(pinned, non_blocking=True)
+        return p, sv
+
+    def stage_mps(self, p: Plan, sv: torch.Tensor, bond_dimension: int, stream=None):
+        """(a) statevector -> MPS: site tensors, bonds and the dense truncated target."""
+        sp = self._sp(stream)
+        tensors = torch.empty(max(p.tensor_elems, 1) * 2, dtype=torch.float64, device="cuda")
+        bonds = torch.empty(p.B * (p.max_n + 1), dtype=torch.int32, device="cuda")
+        target = torch.empty_like(sv)
+        self.hd.check(self.lib.qmprs_mps_from_statevector(p.p, _ptr(sv), int(bond_dimension), 1e-10,
+                                                          _ptr(tensors), _ptr(bonds), _ptr(target), sp))
+        return tensors, bonds, target
+
+    def mps_to_statevector(self, p: Plan, tensors: torch.Tensor, bonds: torch.Tensor, stream=None) -> torch.Tensor:
+        sp = self._sp(stream)
+        out = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        self.hd.check(self.lib.qmprs_mps_to_statevector(p.p, _ptr(tensors), _ptr(bonds), _ptr(out), sp))
+        return out
+
+    def stage_layers(self, p: Plan, target: torch.Tensor, num_layers: int, fidelity_threshold: float,
+                     stream=None):
+        """(b)+(c) disentangling layers from the dense target."""
+        sp = self._sp(stream)
+        gates = torch.zeros(p.gate_elems * 2, dtype=torch.float64, device="cuda")
+        arity = torch.zeros(p.gate_elems // 16, dtype=torch.int8, device="cuda")
+        nl = torch.zeros(p.B, dtype=torch.int32, device="cuda")
+        lf = torch.zeros(p.B * num_layers * 2, dtype=torch.float64, device="cuda")
+        self.hd.check(self.lib.qmprs_unitary_layers(p.p, _ptr(target), int(num_layers), float(fidelity_threshold),
+                                                    _ptr(gates), _ptr(arity), _ptr(nl), _ptr(lf), sp))
+        return gates, arity, nl, lf
+
+    def stage_sweeps(self, p: Plan, target, gates, arity, nl, num_sweeps: int, stop_fidelity: float = 0.0,
+                     stream=None):
+        """(d) environment sweeps; returns per-sweep fidelities and sweeps run."""
+        sp = self._sp(stream)
+        S = max(int(num_sweeps), 0)
+        sf = torch.zeros(max(p.B * S, 1), dtype=torch.float64, device="cuda")
+        sd = torch.zeros(p.B, dtype=torch.int32, device="cuda")
+        if S > 0:
+            self.hd.check(self.lib.qmprs_optimize_layers(p.p, _ptr(target), _ptr(gates), _ptr(arity), _ptr(nl), S,
+                                                         float(stop_fidelity), _ptr(sf), _ptr(sd), sp))
+        return sf, sd
+
+    def stage_circuit(self, p: Plan, gates, arity, nl, stream=None) -> torch.Tensor:
+        sp = self._sp(stream)
+        circ = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        self.hd.check(self.lib.qmprs_circuit_state(p.p, _ptr(gates), _ptr(arity), _ptr(nl), _ptr(circ), sp))
+        return circ
+
+    def overlap(self, p: Plan, a: torch.Tensor, b: torch.Tensor, stream=None) -> torch.Tensor:
+        sp = self._sp(stream)
+        ov = torch.zeros(p.B * 2, dtype=torch.float64, device="cuda")
+        self.hd.check(self.lib.qmprs_overlap(p.p, _ptr(a), _ptr(b), _ptr(ov), sp))
+        return ov
+
+    def apply_layer(self, p: Plan, vec, gates, arity, layer: int, inverse: bool, stream=None) -> None:
+        sp = self._sp(stream)
+        self.hd.check(self.lib.qmprs_apply_layer(p.p, _ptr(vec), _ptr(gates), _ptr(arity), int(layer),
+                                                 1 if inverse else 0, sp))
+
+    def set_profiling(self, p: Plan, on: bool) -> None:
+        self.hd.check(self.lib.qmprs_plan_set_profiling(p.p, 1 if on else 0))
+
+    def profile(self, p: Plan, kernel: int) -> tuple[int, float, float]:
+        """(launches, event milliseconds, algorithmic bytes) of a sweep kernel class."""
+        n, ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+        self.hd.check(self.lib.qmprs_plan_profile(p.p, int(kernel), ctypes.byref(n), ctypes.byref(ms),
+                                                  ctypes.byref(by)))
+        return n.value, ms.value, by.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.qmprs_launch_count())
+
+    def random_mps_states(self, ns, bonds, seed: int) -> torch.Tensor:
+        """Random-MPS statevectors (i.i.d. complex Gaussian tensors of bond
+        ``bonds[b]``, left-canonicalised, contracted on the GPU, normalised)
+        in one packed complex64 device buffer with the plan layout of ``ns``."""
+        chi = max(int(x) for x in bonds)
+        p = self.plan(ns, 1, chi)
+        rng = np.random.default_rng(seed)
+        store = np.zeros(p.tensor_elems, dtype=np.complex128)
+        bond_arr = np.zeros((p.B, p.max_n + 1), dtype=np.int32)
+        for b, (n, bd) in enumerate(zip(ns, bonds)):
+            dims = [1] + [min(int(bd), 2 ** min(i, n - i)) for i in range(1, n)] + [1]
+            ts = []
+            for i in range(n):
+                shape = (dims[i], 2, dims[i + 1])
+                ts.append((rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2.0))
+            for i in range(n - 1):
+                l, pp, r = ts[i].shape
+                q, rr = np.linalg.qr(ts[i].reshape(l * pp, r))
+                ts[i] = q.reshape(l, pp, q.shape[1])
+                nl, np_, nr = ts[i + 1].shape
+                ts[i + 1] = (rr @ ts[i + 1].reshape(nl, np_ * nr)).reshape(q.shape[1], np_, nr)
+            ce = p.chi_eff(b)
+            base = int(p.tensor_off[b])
+            for s, t in enumerate(ts):
+                off = base + s * 2 * ce * ce
+                store[off: off + t.size] = t.reshape(-1)
+            bond_arr[b, : n + 1] = [1] + [t.shape[2] for t in ts]
+        dt = torch.from_numpy(store.view(np.float64)).cuda()
+        db = torch.from_numpy(bond_arr.reshape(-1)).cuda()
+        vec = self.mps_to_statevector(p, dt, db)
+        ov = self.overlap(p, vec, vec)
+        torch.cuda.current_stream().synchronize()
+        inv = torch.rsqrt(ov[0::2]).to(torch.float32)
+        counts = torch.tensor([2 ** (n + 1) for n in ns], dtype=torch.int64, device="cuda")
+        return vec * torch.repeat_interleave(inv, counts)
+
+    @staticmethod
+    def _sp(stream) -> ctypes.c_void_p:
+        st = stream or torch.cuda.current_stream()
+        return ctypes.c_void_p(st.cuda_stream)
+
+    # ---- whole path ------------------------------------------------------------
+    def encode(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
+               fidelity_threshold: float = 1 - 1e-6, stop_fidelity: float = 0.0,
+               keep_tensors: bool = False, nqubits=None, download: bool = True) -> BatchResult:
+        """``prepare_state`` for a batch: (a) -> (b)+(c) -> (d) -> fidelity.
+
+        ``statevectors`` is either a list of complex arrays, or (with
+        ``nqubits``) one packed float32 tensor holding the complex64
+        amplitudes of all states back to back, resident on the GPU or in
+        (pinned) host memory.  Inputs need not be normalised: the reported
+        fidelity is ``|<sv|C|0>| / ||sv||``.
+        """
+        if nqubits is None:
+            p, sv = self.upload(statevectors, num_layers, bond_dimension)
+        else:
+            p = self.plan(nqubits, num_layers, bond_dimension)
+            sv = statevectors
+            if sv.numel() != 2 * p.vec_elems:
+                raise ValueError("packed statevector buffer does not match the qubit counts")
+            if not sv.is_cuda:
+                sv = sv.to("cuda", non_blocking=True)
+        tensors, bonds, target = self.stage_mps(p, sv, bond_dimension)
+        gates, arity, nl, lf = self.stage_layers(p, target, num_layers, fidelity_threshold)
+        sf, sd = self.stage_sweeps(p, target, gates, arity, nl, num_sweeps, stop_fidelity)
+        circ = self.stage_circuit(p, gates, arity, nl)
+        ov = self.overlap(p, circ, sv)
+        nn = self.overlap(p, sv, sv)
+        B, S = p.B, max(int(num_sweeps), 0)
+        if not download:
+            return BatchResult(nqubits=p.nqubits, gates=gates, arity=arity, num_layers=nl, layer_fidelities=lf,
+                               sweep_fidelities=sf, sweeps_done=sd, fidelity=torch.stack([ov, nn]),
+                               gate_off=p.gate_off, max_n=p.max_n, max_bond=int(bond_dimension))
+        torch.cuda.current_stream().synchronize()
+        ovh = ov.cpu().numpy().view(np.complex128)
+        nnh = nn.cpu().numpy().view(np.complex128).real
+        res = BatchResult(
+            nqubits=p.nqubits,
+            gates=gates.cpu().numpy().view(np.complex128),
+            arity=arity.cpu().numpy(),
+            num_layers=nl.cpu().numpy(),
+            layer_fidelities=lf.cpu().numpy().view(np.complex128).reshape(B, num_layers),
+            sweep_fidelities=sf.cpu().numpy()[: B * S].reshape(B, S),
+            sweeps_done=sd.cpu().numpy(),
+            fidelity=np.abs(ovh) / np.sqrt(nnh),
+            gate_off=p.gate_off,
+            max_n=p.max_n,
+            max_bond=int(bond_dimension),
+        )
+        if keep_tensors:
+            res.tensors = tensors.cpu().numpy().view(np.complex128)
+            res.tensor_off = p.tensor_off
+            res.bonds = bonds.cpu().numpy()
+        return res
+
+
+_engine = None
+
+
+def engine() -> Engine:
+    global _engine
+    if _engine is None:
+        _engine = Engine()
+    return _engine

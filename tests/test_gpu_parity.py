@@ -1,0 +1,174 @@
+"""GPU parity against the FP64 oracle (canonical conventions).
+
+Tolerances: the GPU keeps statevectors in complex64 with FP64 reductions, so
+tensor and gate entries agree to ~1e-5 and fidelities to 1e-6 (the bar
+stated for per-sweep fidelity); quantities that are gauge-free (fidelities)
+are compared everywhere, gate entries only where the gauge is fixed
+(non-degenerate random states).
+"""
+
+import copy
+
+import numpy as np
+import pytest
+
+from oracle import dense as D
+from oracle import states as S
+
+pytestmark = pytest.mark.gpu
+
+FID_TOL = 1e-6
+GATE_TOL = 2e-4
+
+
+@pytest.fixture(scope="module")
+def eng(cuda_lib):
+    from qmprs_gb300 import engine
+    return engine.engine()
+
+
+def _svs(ns, seed0=0, fam="uniform"):
+    out = []
+    for i, n in enumerate(ns):
+        if fam == "uniform":
+            out.append(S.uniform_complex(n, seed0 + i))
+        else:
+            out.append(S.random_mps(n, 4, seed0 + i))
+    return out
+
+
+def _oracle_target(sv, chi):
+    n = D.num_qubits(sv)
+    sv64 = sv.astype(np.complex64).astype(np.complex128)
+    return D.mps_to_dense(D.tt_svd_right(sv64 / np.linalg.norm(sv64), n, chi))
+
+
+@pytest.mark.parametrize("ns,chi", [([6], 64), ([8], 4), ([10], 8), ([5, 9, 7], 16), ([12], 32)])
+def test_sv_to_mps(eng, ns, chi):
+    svs = _svs(ns, 3)
+    res = eng.encode(svs, chi, num_layers=1, keep_tensors=True)
+    for b, sv in enumerate(svs):
+        n = ns[b]
+        sv64 = sv.astype(np.complex64).astype(np.complex128)
+        sv64 /= np.linalg.norm(sv64)
+        ref = D.tt_svd_right(sv64, n, chi)
+        got = res.mps_tensors(b)
+        for s in range(n):
+            assert got[s].shape == ref[s].shape, (b, s)
+            assert np.allclose(got[s], ref[s], atol=GATE_TOL), (b, s)
+
+
+def test_untruncated_reconstruction(eng):
+    from qmprs_gb300 import engine as E
+    import torch
+    n = 10
+    sv = S.uniform_complex(n, 7)
+    p, dsv = eng.upload([sv], 1, 32)
+    _, _, target = eng.stage_mps(p, dsv, 32)
+    torch.cuda.synchronize()
+    t = target.cpu().numpy().view(np.complex64).astype(np.complex128)
+    assert np.linalg.norm(t - sv) < 1e-6
+
+
+@pytest.mark.parametrize("ns,L", [([6], 3), ([8], 4), ([5, 8, 11], 3), ([13], 2)])
+def test_layers_match_oracle(eng, ns, L):
+    svs = _svs(ns, 11)
+    res = eng.encode(svs, 64, num_layers=L)
+    for b, sv in enumerate(svs):
+        n = ns[b]
+        t = _oracle_target(sv, 64)
+        layers, fids = D.get_unitary_layers(t, n, L)
+        assert int(res.num_layers[b]) == len(fids)
+        assert np.allclose(res.layer_fidelities[b, : len(fids)], fids, atol=FID_TOL)
+        got = D.circuit_gates(res.layers(b))
+        ref = D.circuit_gates(layers)
+        assert len(got) == len(ref)
+        for a, r in zip(got, ref):
+            assert a[:4] == r[:4]
+        # the first generated layer (last in circuit order) entry by entry; later
+        # layers inherit fp32 rounding amplified by small singular-value gaps,
+        # so they are held to the gauge-free fidelities above
+        for a, r in zip(got[-n:], ref[-n:]):
+            assert np.allclose(a[4], r[4], atol=GATE_TOL)
+
+
+@pytest.mark.parametrize("ns,L,S_", [([6], 3, 4), ([8], 4, 3), ([7, 10], 2, 3), ([12], 3, 2)])
+def test_sweeps_match_oracle(eng, ns, L, S_):
+    """Per-sweep fidelity from identical initial layers (the gauge-free check)."""
+    svs = _svs(ns, 21)
+    res = eng.encode(svs, 64, num_layers=L, num_sweeps=S_)
+    for b, sv in enumerate(svs):
+        n = ns[b]
+        t = _oracle_target(sv, 64)
+        layers, _ = D.get_unitary_layers(t, n, L)
+        fs = []
+        for _ in range(S_):
+            layers, f = D.sweep(t, n, layers)
+            fs.append(f)
+        assert np.allclose(res.sweep_fidelities[b], fs, atol=FID_TOL), (res.sweep_fidelities[b], fs)
+        psi = D.circuit_state(layers, n)
+        assert abs(res.fidelity[b] - abs(np.vdot(psi, sv))) < FID_TOL
+
+
+def test_sweeps_from_given_layers(eng):
+    """_optimize_unitary_layers on oracle-made layers reproduces the oracle sweeps."""
+    from qmprs_gb300.primitives import MPS
+    from qmprs_gb300.circuit import Circuit
+    from qmprs_gb300.synthesis.mps_encoding import Sequential
+    n = 8
+    sv = S.uniform_complex(n, 5)
+    mps = MPS(statevector=sv, bond_dimension=64)
+    t = _oracle_target(sv, 64)
+    layers, _ = D.get_unitary_layers(t, n, 3, mode="literal")
+    seq = Sequential(Circuit)
+    out = seq._optimize_unitary_layers(mps, copy.deepcopy(layers), 4)
+    fs = []
+    ref = copy.deepcopy(layers)
+    for _ in range(4):
+        ref, f = D.sweep(t, n, ref)
+        fs.append(f)
+    assert np.allclose(seq.last_run["sweep_fidelities"], fs, atol=FID_TOL)
+    psi_gpu = D.circuit_state(out, n)
+    assert abs(abs(np.vdot(psi_gpu, sv)) - abs(np.vdot(D.circuit_state(ref, n), sv))) < FID_TOL
+
+
+def test_batch_equals_single(eng):
+    ns = [6, 9, 7, 12]
+    svs = _svs(ns, 31)
+    rb = eng.encode(svs, 32, num_layers=3, num_sweeps=2)
+    for b, sv in enumerate(svs):
+        r1 = eng.encode([sv], 32, num_layers=3, num_sweeps=2)
+        assert np.allclose(rb.sweep_fidelities[b], r1.sweep_fidelities[0], atol=1e-12)
+        assert np.allclose(rb.layer_fidelities[b], r1.layer_fidelities[0], atol=1e-12)
+
+
+def test_deterministic(eng):
+    svs = _svs([10, 11], 41)
+    r1 = eng.encode(svs, 16, num_layers=3, num_sweeps=3)
+    r2 = eng.encode(svs, 16, num_layers=3, num_sweeps=3)
+    assert np.array_equal(r1.gates, r2.gates)
+    assert np.array_equal(r1.sweep_fidelities, r2.sweep_fidelities)
+
+
+def test_exact_states_one_layer(eng):
+    """Bond-2 states are encoded exactly by one layer and stop early."""
+    svs = [S.random_mps(n, 2, n) for n in (4, 9, 14)]
+    res = eng.encode(svs, 64, num_layers=5)
+    assert list(res.num_layers) == [1, 1, 1]
+    assert np.all(res.fidelity > 1 - 1e-5)
+
+
+def test_product_and_zero_states(eng):
+    z = np.zeros(2 ** 6, complex)
+    z[0] = 1
+    plus = np.ones(2 ** 5, complex) / np.sqrt(32)
+    res = eng.encode([z, plus], 8, num_layers=3, num_sweeps=1)
+    assert list(res.num_layers) == [1, 1]
+    assert np.all(res.fidelity > 1 - 1e-6)
+    assert all(len(layer) == n for layer, n in zip([res.layers(0)[0], res.layers(1)[0]], [6, 5]))
+
+
+def test_two_qubits(eng):
+    sv = S.uniform_complex(2, 3)
+    res = eng.encode([sv], 4, num_layers=2, num_sweeps=2)
+    assert res.fidelity[0] > 1 - 1e-6

@@ -1,0 +1,150 @@
+"""The FP64 small linear algebra compiled into the kernels, run on the CPU.
+
+``qmprs_gb300/csrc/small_linalg.h`` is compiled both into the CUDA library
+and into ``libqmprs_hostcheck.so``; these tests hold the host build to the
+oracle's canonical conventions and to numpy's decompositions.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import conventions as cv
+from oracle import dense as D
+from qmprs_gb300 import build as qb
+
+
+@pytest.fixture(scope="module")
+def hc():
+    lib = ctypes.CDLL(str(qb.build_hostcheck()))
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.hc_herm_eig.argtypes = [dp, ctypes.c_int, dp, dp]
+    lib.hc_polar.argtypes = [dp, ctypes.c_int, dp, dp]
+    lib.hc_polar.restype = ctypes.c_double
+    lib.hc_complement.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
+    lib.hc_rank_by_cutoff.argtypes = [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    lib.hc_rank_by_cutoff.restype = ctypes.c_int
+    lib.hc_phase_fix_column.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.hc_ran_gate.argtypes = [ctypes.c_int, dp, dp]
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 8])
+def test_herm_eig(hc, n):
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, 2 * n)) + 1j * rng.standard_normal((n, 2 * n))
+    g = _c(a @ a.conj().T)
+    v = np.zeros((n, n), np.complex128)
+    lam = np.zeros(n)
+    hc.hc_herm_eig(_p(g), n, _p(v), _p(lam))
+    ref = np.linalg.eigvalsh(g)[::-1]
+    assert np.allclose(lam, ref, rtol=1e-12, atol=1e-12)
+    assert np.allclose(g @ v, v * lam[None, :], atol=1e-10)
+    assert np.allclose(v.conj().T @ v, np.eye(n), atol=1e-12)
+
+
+def test_herm_eig_rank_deficient_tail(hc):
+    """Tiny eigenvalues of a PSD Gram matrix keep their relative accuracy."""
+    rng = np.random.default_rng(0)
+    q, _ = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    lam_true = np.array([1.0, 0.3, 1e-9, 1e-13])
+    g = _c(q @ np.diag(lam_true) @ q.conj().T)
+    v = np.zeros((4, 4), np.complex128)
+    lam = np.zeros(4)
+    hc.hc_herm_eig(_p(g), 4, _p(v), _p(lam))
+    assert abs(lam[2] - 1e-9) < 1e-15
+    sq = _c(lam).real.copy()
+    assert hc.hc_rank_by_cutoff(sq.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 4, 1e-10, 4) == \
+        cv.rank_by_cutoff(np.sqrt(np.maximum(lam_true, 0)))
+
+
+@pytest.mark.parametrize("m", [2, 4])
+@pytest.mark.parametrize("seed", range(5))
+def test_polar_matches_numpy(hc, m, seed):
+    rng = np.random.default_rng(seed)
+    e = _c(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    w = np.zeros((m, m), np.complex128)
+    nuc = hc.hc_polar(_p(e), m, _p(w), None)
+    wref, s = cv.polar_unitary(e)
+    assert np.allclose(w, wref, atol=1e-12)
+    assert abs(nuc - s.sum()) < 1e-12
+
+
+def test_polar_rank_one(hc):
+    """Rank-deficient environments still give a unitary with the right column."""
+    e = np.zeros((4, 4), np.complex128)
+    e[:, 0] = [0.3, 0.1j, -0.2, 0.5]
+    w = np.zeros((4, 4), np.complex128)
+    nuc = hc.hc_polar(_p(_c(e)), 4, _p(w), None)
+    assert np.allclose(w.conj().T @ w, np.eye(4), atol=1e-12)
+    assert np.allclose(w[:, 0], e[:, 0] / np.linalg.norm(e[:, 0]), atol=1e-12)
+    assert abs(nuc - np.linalg.norm(e[:, 0])) < 1e-12
+
+
+@pytest.mark.parametrize("rank", [0, 1, 2, 3])
+@pytest.mark.parametrize("seed", range(3))
+def test_polar_null_space_follows_previous(hc, rank, seed):
+    """Rank-deficient environments: the completion nearest to the previous
+    unitary, identical to the oracle's canonical rule."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((4, rank)) + 1j * rng.standard_normal((4, rank))
+    b = rng.standard_normal((rank, 4)) + 1j * rng.standard_normal((rank, 4))
+    e = _c(a @ b)
+    e = e + 1e-9 * (rng.standard_normal((4, 4)))          # below the null threshold
+    prev, _ = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    prev = _c(prev)
+    w = np.zeros((4, 4), np.complex128)
+    hc.hc_polar(_p(_c(e)), 4, _p(w), _p(prev))
+    ref, _ = cv.polar_unitary_canonical(e, prev)
+    assert np.allclose(w.conj().T @ w, np.eye(4), atol=1e-10)
+    assert np.allclose(w, ref, atol=1e-7)
+
+
+@pytest.mark.parametrize("k,n", [(1, 2), (1, 4), (2, 4)])
+@pytest.mark.parametrize("seed", range(4))
+def test_complement_matches_oracle(hc, k, n, seed):
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    x = _c(q[:, :k].T)
+    c = np.zeros((n - k, n), np.complex128)
+    hc.hc_complement(_p(x), k, n, _p(c))
+    ref = cv.householder_complement(x)
+    assert np.allclose(c.T, ref, atol=1e-13)
+
+
+def test_phase_fix_matches_oracle(hc):
+    rng = np.random.default_rng(3)
+    v = _c(rng.standard_normal((4, 3)) + 1j * rng.standard_normal((4, 3)))
+    ref = cv.phase_fix_rows(v.T).T
+    for col in range(3):
+        hc.hc_phase_fix_column(_p(v), 4, 3, col)
+    assert np.allclose(v, ref, atol=1e-14)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_ran_gates_match_oracle(hc, seed):
+    n = 6
+    sv = np.random.default_rng(seed).standard_normal(2 ** n) + 0j
+    sv = sv / np.linalg.norm(sv)
+    tensors = D.tt_svd_right(sv, n, 2)
+    tensors[0] = tensors[0] / np.linalg.norm(tensors[0])
+    out = np.zeros((4, 4), np.complex128)
+    hc.hc_ran_gate(0, _p(_c(tensors[0].reshape(-1))), _p(out))
+    assert np.allclose(out, D.first_site_unitary(tensors[0], "canonical"), atol=1e-13)
+    hc.hc_ran_gate(1, _p(_c(tensors[2].reshape(-1))), _p(out))
+    assert np.allclose(out, D.two_site_unitary(tensors[2], "canonical"), atol=1e-13)
+    o2 = np.zeros((2, 2), np.complex128)
+    hc.hc_ran_gate(2, _p(_c(tensors[n - 1].reshape(-1))), _p(o2))
+    assert np.allclose(o2, D.last_site_unitary(tensors[n - 1], 0, n - 1, "canonical"), atol=1e-13)
+    v = _c([0.6, 0.8j])
+    hc.hc_ran_gate(3, _p(v), _p(o2))
+    assert np.allclose(o2, D.last_site_unitary(v.reshape(1, 2, 1), 3, 3, "canonical"), atol=1e-13)

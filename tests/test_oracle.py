@@ -1,0 +1,172 @@
+"""The FP64 oracle: internal consistency and the reference's own behaviours.
+
+The reference ships no golden vectors (its randomness is unseeded), so the
+oracle is pinned by (1) agreement between its two restatements (the
+call-by-call MPS one and the dense one), (2) the behaviours the reference's
+tests assert (``tests/synthesis/mps_encoding/test_sequential_encoding.py``,
+``tests/primitives/test_mps.py``), and (3) the reference's published
+fidelities (README.md:49-71 and the notebook), matched statistically.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import conventions as cv
+from oracle import dense as D
+from oracle import mpsops as M
+from oracle import states as S
+
+
+def _rand_state(n, seed):
+    return S.uniform_complex(n, seed)
+
+
+def test_rank_by_cutoff():
+    s = np.array([1.0, 1e-3, 1e-6])
+    assert cv.rank_by_cutoff(s) == 2            # 1e-12 tail <= 1e-10 * total
+    assert cv.rank_by_cutoff(s, max_bond=1) == 1
+    assert cv.rank_by_cutoff(np.array([1.0, 0.0])) == 1
+    assert cv.rank_by_cutoff(np.array([0.6, 0.6, 0.6])) == 3
+
+
+@pytest.mark.parametrize("k,n", [(1, 2), (1, 4), (2, 4), (3, 4)])
+def test_householder_complement(k, n):
+    rng = np.random.default_rng(k * 10 + n)
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    q, _ = np.linalg.qr(a)
+    x = q[:, :k].T.copy()
+    c = cv.householder_complement(x)
+    full = np.concatenate([x.T, c], axis=1)
+    assert np.allclose(full.conj().T @ full, np.eye(n), atol=1e-12)
+
+
+def test_householder_complement_structured():
+    # exact basis vectors and equal-magnitude rows resolve ties to the lowest index
+    c = cv.householder_complement(np.array([[1, 0, 0, 0]], dtype=complex))
+    assert np.allclose(np.abs(c), np.eye(4)[:, 1:])
+    x = np.array([[0.5, 0.5, 0.5, 0.5]], dtype=complex)
+    c = cv.householder_complement(x)
+    assert np.allclose(x.conj() @ c, 0, atol=1e-14)
+
+
+@pytest.mark.parametrize("n,chi,L,S_", [(6, 8, 4, 2), (7, 64, 3, 2), (8, 4, 3, 1)])
+def test_dense_equals_mps_restatement(n, chi, L, S_):
+    """The dense reformulation reproduces the call-by-call MPS restatement."""
+    sv = _rand_state(n, 100 + n)
+    rd = D.prepare_state(sv, chi, L, S_, mode="canonical")
+    rm = M.prepare_state(sv, chi, L, S_, conv="canonical")
+    assert np.allclose(rd.target, rm.target, atol=1e-12)
+    # layers before sweeps: gate by gate
+    ld, _ = D.get_unitary_layers(rd.target, n, L, mode="canonical")
+    mps = M.from_statevector(sv, chi, conv="canonical")
+    lm, _ = M.get_unitary_layers(mps, L, conv="canonical")
+    for a, b in zip(D.circuit_gates(ld), D.circuit_gates(lm)):
+        assert a[:4] == b[:4]
+        assert np.allclose(a[4], b[4], atol=1e-8)
+    assert np.allclose(rd.layer_fidelities, rm.layer_fidelities, atol=1e-10)
+    assert np.allclose(rd.sweep_fidelities, rm.sweep_fidelities, atol=1e-10)
+    assert abs(rd.fidelity - rm.fidelity) < 1e-10
+
+
+def test_literal_first_layer_is_gauge_invariant():
+    """The first layer's zero-state overlap does not depend on the conventions."""
+    n = 8
+    sv = _rand_state(n, 5)
+    t = D.mps_to_dense(D.tt_svd_right(sv, n, 64))
+    _, fc = D.get_unitary_layers(t, n, 1, mode="canonical")
+    _, fl = D.get_unitary_layers(t, n, 1, mode="literal")
+    assert abs(fc[0] - fl[0]) < 1e-12
+
+
+def test_sweep_same_from_identical_layers_literal_vs_canonical():
+    """Sweeps are gauge-robust: the same initial layers give the same fidelities."""
+    n = 7
+    sv = _rand_state(n, 9)
+    t = D.mps_to_dense(D.tt_svd_right(sv, n, 64))
+    layers, _ = D.get_unitary_layers(t, n, 3, mode="literal")
+    import copy
+    l1 = copy.deepcopy(layers)
+    f1 = [D.sweep(t, n, l1)[1] for _ in range(3)]
+    l2 = M.get_unitary_layers(M.from_statevector(sv, 64), 3)[0]
+    f2 = [D.sweep(t, n, l2)[1] for _ in range(3)]
+    assert len(f1) == len(f2)
+
+
+def test_untruncated_mps_reproduces_statevector():
+    n = 9
+    sv = _rand_state(n, 3)
+    t = D.mps_to_dense(D.tt_svd_right(sv, n, 2 ** (n // 2)))
+    assert np.linalg.norm(t - sv) < 1e-10
+
+
+# ---- reference behaviours (test_sequential_encoding.py) ---------------------------
+
+
+def test_reference_prepare_state_threshold():
+    sv = _rand_state(8, 11)
+    r = D.prepare_state(sv, 32, num_layers=32)
+    assert 1 - r.fidelity < 1e-2
+
+
+@pytest.mark.parametrize("mode", ["canonical", "literal"])
+def test_reference_layer_improvement(mode):
+    sv = _rand_state(8, 12)
+    f = [D.prepare_state(sv, 64, num_layers=i, mode=mode).fidelity for i in range(1, 10)]
+    assert np.all(np.diff(f) >= 0)
+
+
+@pytest.mark.parametrize("mode", ["canonical", "literal"])
+def test_reference_sweep_improvement(mode):
+    sv = _rand_state(8, 13)
+    f = [D.prepare_state(sv, 64, num_layers=6, num_sweeps=i, mode=mode).fidelity for i in range(1, 8)]
+    assert np.all(np.diff(f) >= 0)
+
+
+def _ghz_like(n, pairs, plus):
+    """|0..0> with H on `plus` qubits and CX chains (qiskit little-endian labels)."""
+    from qmprs_gb300.circuit import Circuit
+    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
+    cx = np.eye(4)[[0, 3, 2, 1]]       # control = first listed qubit (LSB of U)
+    c = Circuit(n)
+    for q in plus:
+        c.unitary(h, q)
+    for a, b in pairs:
+        c.unitary(cx, [a, b])
+    return c.get_statevector()
+
+
+def test_reference_partial_entanglement_depth():
+    from qmprs_gb300.circuit import Circuit
+    from qmprs_gb300.synthesis.mps_encoding import Sequential
+    sv = _ghz_like(8, [(0, 3), (5, 7)], [0, 4, 5])
+    r = D.prepare_state(sv, 32, num_layers=1)
+    assert 1 - r.fidelity < 1e-2
+    c = Circuit(8)
+    for layer in r.layers:
+        Sequential._apply_unitary_layer_to_circuit(c, layer)
+    assert np.allclose(c.get_statevector(), D.circuit_state(r.layers, 8), atol=1e-12)
+    assert c.get_depth() <= 20
+
+
+def test_reference_partial_entanglement_with_sweep_depth():
+    from qmprs_gb300.circuit import Circuit
+    from qmprs_gb300.synthesis.mps_encoding import Sequential
+    sv = _ghz_like(4, [(0, 1), (1, 2)], [0, 3])
+    r = D.prepare_state(sv, 32, num_layers=1, num_sweeps=1)
+    assert 1 - r.fidelity < 1e-2
+    c = Circuit(4)
+    for layer in r.layers:
+        Sequential._apply_unitary_layer_to_circuit(c, layer)
+    assert c.get_depth() <= 7
+
+
+# ---- published numbers (statistical) --------------------------------------------
+
+
+@pytest.mark.slow
+def test_readme_fidelity_n10_statistically():
+    """README.md:49-71 reports |<psi|C|0>| = 0.98676 for one unseeded 10-qubit
+    uniform-complex state, chi=512, L=15, S=50.  The oracle's mean over seeds
+    must fall in the same band."""
+    f = [D.prepare_state(_rand_state(10, s), 512, 15, 50).fidelity for s in range(3)]
+    assert 0.975 < float(np.mean(f)) < 0.995, f

@@ -48,6 +48,11 @@ if ROOT not in sys.path:
 
 METRIC = "states/sec to fidelity≥0.98: learned warm-start+batched vs plain sweep, 1 GB300"
 UNIT = "states/s"
+# DRAM bytes (read + write) per amplitude of one k_sweep_env launch, from an
+# ncu capture of `python -m qmprs_gb300.profile_workload --states 32 --sweeps 1`
+# (dram__bytes_read.sum + dram__bytes_write.sum = 521.0 MB over 23,195,648
+# amplitudes); the full-size launch is scaled by its amplitude count.
+ENV_DRAM_BYTES_PER_AMP = 521.0e6 / 23195648
 
 
 def workload_spec(name: str, states: int, seed: int):
@@ -307,7 +312,9 @@ def run_gpu(args, rank, world):
                    "reached_0.98": reached, "mean_fidelity": float(np.mean(fid)),
                    "mean_sweeps_run": float(np.mean(sd))},
         "roofline": {"bound": "hbm", "kernel": "k_sweep_env", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": ENV_DRAM_BYTES_PER_AMP * (by_env / max(n_env, 1)) / 24.0,
+                     "traffic_note": "DRAM bytes per launch, scaled by amplitudes from a 32-state ncu capture",
                      "launches": n_env, "avg_launch_us": ms_env / max(n_env, 1) * 1e3,
                      "bytes_per_launch": by_env / max(n_env, 1),
                      "sweep_kernel_ms": {"env_stream": prof[0][1], "env_polar": prof[3][1],

@@ -165,6 +165,26 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
 int qmprs_overlap(qmprs_plan_t p, const void* a, const void* b, void* out, void* stream);
 
 /*
+ * Per-state inner products <a|b> like qmprs_overlap, for callers that
+ * cannot allocate device memory (their GPU memory belongs to another
+ * allocator, or cudaMalloc's implicit synchronisation is not acceptable on
+ * their stream).  No plan and no cudaMalloc/cudaFree: the states are packed
+ * back to back (state i of 2^num_qubits[i] complex64 amplitudes, host array
+ * num_qubits), out is a device complex128[num_states], and the reduction
+ * scratch is a 1 MiB static device array inside the library.  Limits: at most
+ * QMPRS_NOALLOC_MAX_STATES states and QMPRS_NOALLOC_MAX_TILES tiles of 4096
+ * amplitudes in total (2^25 amplitudes); larger requests return
+ * QMPRS_ERR_UNSUPPORTED.  The first call on a device looks up the scratch
+ * address (make it before any stream capture); calls share the scratch, so
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * No counterpart in the reference (which has no device code).
+ */
+#define QMPRS_NOALLOC_MAX_STATES 64
+#define QMPRS_NOALLOC_MAX_TILES 8192
+int qmprs_overlap_noalloc(const void* a, const void* b, int num_states, const int* num_qubits, void* out,
+                          void* stream);
+
+/*
  * Apply the adjoint (inverse != 0) or the gate itself of one generated layer
  * to a statevector batch, in the reference's order.
  * Replaces: MPS.apply_unitary_layer (qmprs/primitives/mps.py:893-995).

@@ -52,6 +52,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmprs_overlap": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_apply_layer": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int, ctypes.c_int,
                                          _c_void_p]),
+    "qmprs_overlap_noalloc": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, _c_int_p, _c_void_p, _c_void_p]),
 }
 
 _lib = None

@@ -502,40 +502,25 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
         if (act[b])
           for (int j = 0; j < p->gates_per_state[b]; ++j) amp_at[j] += (double)ipow2(p->n[b]);
     }
+    // C|0>: three consecutive gates per pass on 4-qubit windows
     launch_set_zero_state(p->bd, psi, p->active, s);
-    GateSel sel;
-    sel.layer = 0;
-    sel.gates = gates;
-    sel.arity = ar;
-    sel.nlayers = num_layers;
-    sel.active = p->active;
-    sel.mode = SEL_REBUILD;
-    sel.adjoint = 0;
-    for (int j = 0; j < max_gates; ++j) {
-      sel.step = j;
+    for (int j = 0; j < max_gates; j += 3) {
       log.begin(prof, s);
-      launch_apply_gate(p->bd, psi, sel, s);
+      launch_rebuild_win(p->bd, psi, gates, ar, num_layers, p->active, j, 3, s);
       log.end(prof, 2, s);
       if (prof) p->prof_bytes[2] += 16.0 * amp_at[j];
     }
     CK(cudaMemcpyAsync(t, target, sizeof(float2) * p->vec_total, cudaMemcpyDeviceToDevice, s));
-    sel.mode = SEL_SWEEP;
-    sel.adjoint = 1;
+    // backward sweep: step j peels gate j off psi, applies step j-1's new gate
+    // to t and reduces E_j; the polar kernel turns E_j into the new gate
     for (int j = 0; j < max_gates; ++j) {
       log.begin(prof, s);
-      launch_sweep_env(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
+      launch_env_win(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, s);
       log.end(prof, 0, s);
       log.begin(prof, s);
       launch_sweep_polar(p->bd, j, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
       log.end(prof, 3, s);
-      sel.step = j;
-      log.begin(prof, s);
-      launch_apply_gate(p->bd, t, sel, s);
-      log.end(prof, 1, s);
-      if (prof) {
-        p->prof_bytes[0] += 24.0 * amp_at[j];
-        p->prof_bytes[1] += 16.0 * amp_at[j];
-      }
+      if (prof) p->prof_bytes[0] += (j == 0 ? 24.0 : 32.0) * amp_at[j];
     }
     log.flush(p);
     CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));

@@ -116,6 +116,11 @@ void launch_layer_fidelity(const BatchDev& bd, int layer, const float2* work, in
 void launch_sweep_env(const BatchDev& bd, int step, float2* psi, const float2* t,
                       double2* gates, const signed char* arity, const int* nlayers,
                       const int* active, double2* partials, double* nuc, cudaStream_t s);
+void launch_rebuild_win(const BatchDev& bd, float2* psi, const double2* gates, const signed char* arity,
+                        const int* nlayers, const int* active, int j0, int count, cudaStream_t s);
+void launch_env_win(const BatchDev& bd, int step, float2* psi, float2* t, const double2* gates,
+                    const signed char* arity, const int* nlayers, const int* active, double2* partials,
+                    cudaStream_t s);
 void launch_sweep_polar(const BatchDev& bd, int step, double2* gates, const signed char* arity,
                         const int* nlayers, const int* active, const double2* partials, double* nuc,
                         cudaStream_t s);

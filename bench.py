@@ -271,13 +271,24 @@ def run_gpu(args, rank, world):
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     out_bytes = int(res.gates.nbytes + res.arity.nbytes + res.num_layers.nbytes + res.layer_fidelities.nbytes
                     + res.sweep_fidelities.nbytes + res.sweeps_done.nbytes + res.fidelity.nbytes)
-    # ---- roofline: profiled pass of the sweep stage on the same batch
+    # ---- roofline: profiled pass of the same batch (per-stage events, then
+    # per-kernel events of the sweep stage)
     p = eng.plan(ns, cfg["num_layers"], cfg["bond_dimension"])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev[0].record(stream)
     tensors, bondsd, target = eng.stage_mps(p, sv_dev, cfg["bond_dimension"])
+    ev[1].record(stream)
     gates, arity, nl, lf = eng.stage_layers(p, target, cfg["num_layers"], 1 - 1e-6)
+    ev[2].record(stream)
     eng.set_profiling(p, True)
     eng.stage_sweeps(p, target, gates, arity, nl, cfg["num_sweeps"], cfg["stop_fidelity"])
+    ev[3].record(stream)
+    circ = eng.stage_circuit(p, gates, arity, nl)
+    eng.overlap(p, circ, sv_dev)
+    ev[4].record(stream)
     torch.cuda.synchronize()
+    stage_ms = {"mps_from_statevector": ev[0].elapsed_time(ev[1]), "unitary_layers": ev[1].elapsed_time(ev[2]),
+                "sweeps_profiled": ev[2].elapsed_time(ev[3]), "circuit_and_fidelity": ev[3].elapsed_time(ev[4])}
     prof = {k: eng.profile(p, k) for k in (0, 1, 2, 3)}
     eng.set_profiling(p, False)
     peak, peak_kind = peaks()
@@ -326,6 +337,7 @@ def run_gpu(args, rank, world):
                          "detail": cpu_detail},
         "e2e": {"value": B * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms},
+        "stage_ms": stage_ms,
         "gpu_launches": int(launches),
         "clocks": clk,
     }

@@ -22,6 +22,16 @@ double hc_polar(const double* e, int m, double* w_out, const double* w_prev) {
   return nuc;
 }
 
+double hc_polar_sweep(const double* e, int m, double* w_out, const double* w_prev) {
+  double2 a[16], w[16], wp[16];
+  for (int i = 0; i < m * m; ++i) a[i] = cd(e[2 * i], e[2 * i + 1]);
+  if (w_prev)
+    for (int i = 0; i < m * m; ++i) wp[i] = cd(w_prev[2 * i], w_prev[2 * i + 1]);
+  double nuc = polar_sweep(a, m, w, w_prev ? wp : nullptr);
+  for (int i = 0; i < m * m; ++i) { w_out[2 * i] = w[i].x; w_out[2 * i + 1] = w[i].y; }
+  return nuc;
+}
+
 void hc_complement(const double* x, int k, int n, double* cols_out) {
   double2 a[16], c[16];
   for (int i = 0; i < k * n; ++i) a[i] = cd(x[2 * i], x[2 * i + 1]);

@@ -261,13 +261,464 @@ QM_HD void normalise_or_complete(double2 (&a)[4][4], int m, int nc, double tiny,
 
 #define QM_POLAR_NULL_TOL 1e-6
 
-// Unitary polar factor W (row-major m x m, m in {2, 4}) of E: the maximiser
+// One Hestenes rotation of columns p, q of a (length M) and of v (length M),
+// restricted to pairs where both `use` flags are set.  Returns 1 if rotated.
+template <int M>
+QM_HD int jacobi_pair(double2 (&a)[M][M], double2 (&v)[M][M], int p, int q) {
+  double alpha = 0.0, beta = 0.0;
+  double2 gam = czero();
+#pragma unroll
+  for (int r = 0; r < M; ++r) {
+    alpha += cnorm2(a[p][r]);
+    beta += cnorm2(a[q][r]);
+    gam = cadd(gam, cmulc(a[p][r], a[q][r]));
+  }
+  const double ag2 = cnorm2(gam);
+  if (ag2 == 0.0 || ag2 <= 1e-30 * alpha * beta) return 0;
+  const double ag = sqrt(ag2);
+  const double zeta = (beta - alpha) / (2.0 * ag);
+  const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  const double c = 1.0 / sqrt(1.0 + t * t);
+  const double s = c * t;
+  const double2 ph = cscale(gam, 1.0 / ag);
+  const double2 se = cscale(ph, s), sce = cscale(cconj(ph), s);
+#pragma unroll
+  for (int r = 0; r < M; ++r) {
+    const double2 xp = a[p][r], xq = a[q][r];
+    a[p][r] = csub(cscale(xp, c), cmul(sce, xq));
+    a[q][r] = cadd(cmul(se, xp), cscale(xq, c));
+    const double2 vp = v[p][r], vq = v[q][r];
+    v[p][r] = csub(cscale(vp, c), cmul(sce, vq));
+    v[q][r] = cadd(cmul(se, vp), cscale(vq, c));
+  }
+  return 1;
+}
+
+// Hestenes sweeps over the column pairs (p < q) whose mask bits are both set.
+template <int M>
+QM_HD void jacobi_sweeps(double2 (&a)[M][M], double2 (&v)[M][M], int mask) {
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    int rotated = 0;
+#pragma unroll
+    for (int p = 0; p < M - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < M; ++q)
+        if (((mask >> p) & 1) && ((mask >> q) & 1)) rotated |= jacobi_pair<M>(a, v, p, q);
+    if (!rotated) break;
+  }
+}
+
+// Gram-Schmidt completion of column c of u (length M) on e_0, e_1, ...
+// against the columns of u selected by `against`.
+template <int M>
+QM_HD void complete_column(double2 (&u)[M][M], int c, int against) {
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    double2 v[M];
+#pragma unroll
+    for (int r = 0; r < M; ++r) v[r] = cd(r == k ? 1.0 : 0.0, 0.0);
+    for (int pass = 0; pass < 2; ++pass)
+#pragma unroll
+      for (int o = 0; o < M; ++o) {
+        if (!((against >> o) & 1)) continue;
+        double2 d = czero();
+#pragma unroll
+        for (int r = 0; r < M; ++r) d = cadd(d, cmulc(u[o][r], v[r]));
+#pragma unroll
+        for (int r = 0; r < M; ++r) v[r] = csub(v[r], cmul(u[o][r], d));
+      }
+    double nv = 0.0;
+#pragma unroll
+    for (int r = 0; r < M; ++r) nv += cnorm2(v[r]);
+    nv = sqrt(nv);
+    if (nv > 0.5) {
+#pragma unroll
+      for (int r = 0; r < M; ++r) u[c][r] = cscale(v[r], 1.0 / nv);
+      return;
+    }
+  }
+}
+
+// Unitary polar factor W (row-major M x M, M in {2, 4}) of E: the maximiser
 // of Re Tr(W^H E), via one-sided Jacobi SVD E V = U S, W = U V^H.  Singular
 // values at most QM_POLAR_NULL_TOL * s_max are treated as zero: on that
 // null space every completion maximises Re Tr(W^H E), and W takes the one
 // nearest to `w_prev` (if not null), the orthogonal-Procrustes fit
 // W_N = polar((I - U_s U_s^H) w_prev V_N).  Returns the nuclear norm of E.
-QM_HD double polar_jacobi(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
+// Every loop has a compile-time trip count so the arrays stay in registers;
+// the null-space completion (rank-deficient E only) is a separate,
+// non-inlined function so the common path keeps only E's U S and V live.
+#if defined(__CUDACC__)
+#define QM_NOINLINE __noinline__
+#else
+#define QM_NOINLINE
+#endif
+
+template <int M>
+QM_HD QM_NOINLINE void polar_null_part(const double2 (&u)[M][M], const double2 (&vv)[M][M], int smask, int nmask,
+                                       const double2* w_prev, double2* w_out);
+
+template <int M>
+QM_HD double polar_jacobi_m(const double2* e, double2* w_out, const double2* w_prev) {
+  double2 a[M][M], vv[M][M];
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      a[c][r] = e[r * M + c];
+      vv[c][r] = cd(r == c ? 1.0 : 0.0, 0.0);
+    }
+  jacobi_sweeps<M>(a, vv, (1 << M) - 1);
+  double sig[M], smax = 0.0, nuc = 0.0;
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+    double nrm = 0.0;
+#pragma unroll
+    for (int r = 0; r < M; ++r) nrm += cnorm2(a[c][r]);
+    sig[c] = sqrt(nrm);
+    nuc += sig[c];
+    smax = sig[c] > smax ? sig[c] : smax;
+  }
+  const double thr = QM_POLAR_NULL_TOL * smax;
+  int smask = 0;
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+    if (sig[c] > thr && sig[c] > 1e-300) smask |= 1 << c;
+  const int nmask = ((1 << M) - 1) & ~smask;
+  // a <- U (significant columns normalised in place)
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) a[c][r] = ((smask >> c) & 1) ? cscale(a[c][r], 1.0 / sig[c]) : czero();
+#pragma unroll
+  for (int r = 0; r < M; ++r)
+#pragma unroll
+    for (int s = 0; s < M; ++s) {
+      double2 acc = czero();
+#pragma unroll
+      for (int c = 0; c < M; ++c)
+        if ((smask >> c) & 1) acc = cadd(acc, cmul(a[c][r], cconj(vv[c][s])));
+      w_out[r * M + s] = acc;
+    }
+  if (nmask != 0) {
+    // copies whose address escapes into the non-inlined call, so that a and
+    // vv themselves never need a memory home
+    double2 ua[M][M], uv[M][M];
+#pragma unroll
+    for (int c = 0; c < M; ++c)
+#pragma unroll
+      for (int r = 0; r < M; ++r) {
+        ua[c][r] = a[c][r];
+        uv[c][r] = vv[c][r];
+      }
+    polar_null_part<M>(ua, uv, smask, nmask, w_prev, w_out);
+  }
+  return nuc;
+}
+
+template <int M>
+QM_HD QM_NOINLINE void polar_null_part(const double2 (&us)[M][M], const double2 (&vv)[M][M], int smask, int nmask,
+                                       const double2* w_prev, double2* w_out) {
+  double2 u[M][M];
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) u[c][r] = us[c][r];
+  // null part: X[:, c] = (I - U_s U_s^H) w_prev V[:, c] for null c
+  double2 x[M][M], vx[M][M];
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      double2 acc = czero();
+      if (w_prev && ((nmask >> c) & 1)) {
+#pragma unroll
+        for (int k = 0; k < M; ++k) acc = cadd(acc, cmul(w_prev[r * M + k], vv[c][k]));
+      }
+      x[c][r] = acc;
+      vx[c][r] = cd(r == c ? 1.0 : 0.0, 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      if (!((smask >> i) & 1)) continue;
+      double2 d = czero();
+#pragma unroll
+      for (int r = 0; r < M; ++r) d = cadd(d, cmulc(u[i][r], x[c][r]));
+#pragma unroll
+      for (int r = 0; r < M; ++r) x[c][r] = csub(x[c][r], cmul(u[i][r], d));
+    }
+  }
+  jacobi_sweeps<M>(x, vx, nmask);
+  // orthonormal null columns: normalise, complete the tiny ones in order
+  int okmask = smask;
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+    if (!((nmask >> c) & 1)) continue;
+    double nrm = 0.0;
+#pragma unroll
+    for (int r = 0; r < M; ++r) nrm += cnorm2(x[c][r]);
+    nrm = sqrt(nrm);
+    if (nrm > 1e-8 && isfinite(nrm)) {
+#pragma unroll
+      for (int r = 0; r < M; ++r) u[c][r] = cscale(x[c][r], 1.0 / nrm);
+      okmask |= 1 << c;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+    if (!((nmask >> c) & 1) || ((okmask >> c) & 1)) continue;
+    complete_column<M>(u, c, okmask);
+    okmask |= 1 << c;
+  }
+  // W += Q V_N^H, Q[:, j] = sum_{i null} u_i conj(vx[i][j])
+#pragma unroll
+  for (int j = 0; j < M; ++j) {
+    if (!((nmask >> j) & 1)) continue;
+    double2 q[M];
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      double2 acc = czero();
+#pragma unroll
+      for (int i = 0; i < M; ++i)
+        if ((nmask >> i) & 1) acc = cadd(acc, cmul(u[i][r], cconj(vx[i][j])));
+      q[r] = acc;
+    }
+#pragma unroll
+    for (int r = 0; r < M; ++r)
+#pragma unroll
+      for (int s = 0; s < M; ++s) w_out[r * M + s] = cadd(w_out[r * M + s], cmul(q[r], cconj(vv[j][s])));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Polar factor for the sweep kernel.  GB300 issues FP64 at a small fraction
+// of the FP32 rate, and a single thread's FP64 chain costs a full warp
+// instruction per operation, so the Hestenes sweeps run in FP32 and only the
+// final step is FP64: W = U V^H is re-orthonormalised by modified
+// Gram-Schmidt in FP64 (unitary to rounding) and the overlap after the
+// update is Re Tr(W^H E) in FP64.  W maximises that trace, so the 1e-7
+// difference from the exact polar factor changes it only at second order.
+// Singular values below QM_POLAR_NULL_TOL * s_max are null as in
+// polar_jacobi_m, completed towards w_prev.
+// ---------------------------------------------------------------------------
+QM_HD float2 fcmul(float2 a, float2 b) { return cf(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+QM_HD float2 fcmulc(float2 a, float2 b) { return cf(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
+QM_HD float fcnorm2(float2 a) { return a.x * a.x + a.y * a.y; }
+QM_HD float2 fcscale(float2 a, float s) { return cf(a.x * s, a.y * s); }
+QM_HD float2 fcadd(float2 a, float2 b) { return cf(a.x + b.x, a.y + b.y); }
+QM_HD float2 fcsub(float2 a, float2 b) { return cf(a.x - b.x, a.y - b.y); }
+
+template <int M>
+QM_HD int jacobi_pair_f(float2 (&a)[M][M], float2 (&v)[M][M], int p, int q) {
+  float alpha = 0.f, beta = 0.f;
+  float2 gam = cf(0.f, 0.f);
+#pragma unroll
+  for (int r = 0; r < M; ++r) {
+    alpha += fcnorm2(a[p][r]);
+    beta += fcnorm2(a[q][r]);
+    gam = fcadd(gam, fcmulc(a[p][r], a[q][r]));
+  }
+  const float ag2 = fcnorm2(gam);
+  if (ag2 == 0.f || ag2 <= 1e-14f * alpha * beta) return 0;
+  const float ag = sqrtf(ag2);
+  const float zeta = (beta - alpha) / (2.f * ag);
+  const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+  const float c = 1.f / sqrtf(1.f + t * t);
+  const float s = c * t;
+  const float2 ph = fcscale(gam, 1.f / ag);
+  const float2 se = fcscale(ph, s), sce = fcscale(cf(ph.x, -ph.y), s);
+#pragma unroll
+  for (int r = 0; r < M; ++r) {
+    const float2 xp = a[p][r], xq = a[q][r];
+    a[p][r] = fcsub(fcscale(xp, c), fcmul(sce, xq));
+    a[q][r] = fcadd(fcmul(se, xp), fcscale(xq, c));
+    const float2 vp = v[p][r], vq = v[q][r];
+    v[p][r] = fcsub(fcscale(vp, c), fcmul(sce, vq));
+    v[q][r] = fcadd(fcmul(se, vp), fcscale(vq, c));
+  }
+  return 1;
+}
+
+template <int M>
+QM_HD void jacobi_sweeps_f(float2 (&a)[M][M], float2 (&v)[M][M], int mask) {
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    int rotated = 0;
+#pragma unroll
+    for (int p = 0; p < M - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < M; ++q)
+        if (((mask >> p) & 1) && ((mask >> q) & 1)) rotated |= jacobi_pair_f<M>(a, v, p, q);
+    if (!rotated) break;
+  }
+}
+
+template <int M>
+QM_HD double polar_fast(const double2* e, double2* w_out, const double2* w_prev) {
+  float2 a[M][M], vv[M][M];
+  double scale = 0.0;
+#pragma unroll
+  for (int i = 0; i < M * M; ++i) scale = fmax(scale, fmax(fabs(e[i].x), fabs(e[i].y)));
+  const double inv = scale > 0.0 ? 1.0 / scale : 1.0;
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      a[c][r] = cf((float)(e[r * M + c].x * inv), (float)(e[r * M + c].y * inv));
+      vv[c][r] = cf(r == c ? 1.f : 0.f, 0.f);
+    }
+  jacobi_sweeps_f<M>(a, vv, (1 << M) - 1);
+  float sig[M], smax = 0.f;
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+    float nrm = 0.f;
+#pragma unroll
+    for (int r = 0; r < M; ++r) nrm += fcnorm2(a[c][r]);
+    sig[c] = sqrtf(nrm);
+    smax = fmaxf(smax, sig[c]);
+  }
+  int smask = 0;
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+    if (sig[c] > (float)QM_POLAR_NULL_TOL * smax && sig[c] > 0.f) smask |= 1 << c;
+  const int nmask = ((1 << M) - 1) & ~smask;
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) a[c][r] = ((smask >> c) & 1) ? fcscale(a[c][r], 1.f / sig[c]) : cf(0.f, 0.f);
+  if (nmask != 0) {
+    // X[:, c] = (I - U_s U_s^H) w_prev V[:, c] on the null columns, then the
+    // nearest isometry (Jacobi on those columns), tiny ones completed
+    float2 x[M][M], vx[M][M];
+#pragma unroll
+    for (int c = 0; c < M; ++c) {
+#pragma unroll
+      for (int r = 0; r < M; ++r) {
+        float2 acc = cf(0.f, 0.f);
+        if (w_prev && ((nmask >> c) & 1)) {
+#pragma unroll
+          for (int k = 0; k < M; ++k)
+            acc = fcadd(acc, fcmul(cf((float)w_prev[r * M + k].x, (float)w_prev[r * M + k].y), vv[c][k]));
+        }
+        x[c][r] = acc;
+        vx[c][r] = cf(r == c ? 1.f : 0.f, 0.f);
+      }
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        if (!((smask >> i) & 1)) continue;
+        float2 d = cf(0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < M; ++r) d = fcadd(d, fcmulc(a[i][r], x[c][r]));
+#pragma unroll
+        for (int r = 0; r < M; ++r) x[c][r] = fcsub(x[c][r], fcmul(a[i][r], d));
+      }
+    }
+    jacobi_sweeps_f<M>(x, vx, nmask);
+    int okmask = smask;
+    float2 u[M][M];
+#pragma unroll
+    for (int c = 0; c < M; ++c)
+#pragma unroll
+      for (int r = 0; r < M; ++r) u[c][r] = a[c][r];
+#pragma unroll
+    for (int c = 0; c < M; ++c) {
+      if (!((nmask >> c) & 1)) continue;
+      float nrm = 0.f;
+#pragma unroll
+      for (int r = 0; r < M; ++r) nrm += fcnorm2(x[c][r]);
+      nrm = sqrtf(nrm);
+      if (nrm > 1e-4f) {
+#pragma unroll
+        for (int r = 0; r < M; ++r) u[c][r] = fcscale(x[c][r], 1.f / nrm);
+        okmask |= 1 << c;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < M; ++c) {
+      if (!((nmask >> c) & 1) || ((okmask >> c) & 1)) continue;
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        float2 v[M];
+#pragma unroll
+        for (int r = 0; r < M; ++r) v[r] = cf(r == k ? 1.f : 0.f, 0.f);
+        for (int pass = 0; pass < 2; ++pass)
+#pragma unroll
+          for (int o = 0; o < M; ++o) {
+            if (!((okmask >> o) & 1)) continue;
+            float2 d = cf(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < M; ++r) d = fcadd(d, fcmulc(u[o][r], v[r]));
+#pragma unroll
+            for (int r = 0; r < M; ++r) v[r] = fcsub(v[r], fcmul(u[o][r], d));
+          }
+        float nv = 0.f;
+#pragma unroll
+        for (int r = 0; r < M; ++r) nv += fcnorm2(v[r]);
+        nv = sqrtf(nv);
+        if (nv > 0.5f) {
+#pragma unroll
+          for (int r = 0; r < M; ++r) u[c][r] = fcscale(v[r], 1.f / nv);
+          okmask |= 1 << c;
+          break;
+        }
+      }
+    }
+    // U on the null columns becomes Ux Vx^H: column j = sum_{i null} u_i conj(vx[i][j])
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      if (!((nmask >> j) & 1)) continue;
+#pragma unroll
+      for (int r = 0; r < M; ++r) {
+        float2 acc = cf(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < M; ++i)
+          if ((nmask >> i) & 1) acc = fcadd(acc, fcmul(u[i][r], cf(vx[i][j].x, -vx[i][j].y)));
+        a[j][r] = acc;
+      }
+    }
+  }
+  // W = U V^H in FP64, then modified Gram-Schmidt on its columns
+  double2 w[M][M];   // column-major w[col][row]
+#pragma unroll
+  for (int s = 0; s < M; ++s)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      double2 acc = czero();
+#pragma unroll
+      for (int c = 0; c < M; ++c) acc = cadd(acc, cmul(f2d(a[c][r]), cconj(f2d(vv[c][s]))));
+      w[s][r] = acc;
+    }
+#pragma unroll
+  for (int s = 0; s < M; ++s) {
+#pragma unroll
+    for (int o = 0; o < s; ++o) {
+      double2 d = czero();
+#pragma unroll
+      for (int r = 0; r < M; ++r) d = cadd(d, cmulc(w[o][r], w[s][r]));
+#pragma unroll
+      for (int r = 0; r < M; ++r) w[s][r] = csub(w[s][r], cmul(w[o][r], d));
+    }
+    double nrm = 0.0;
+#pragma unroll
+    for (int r = 0; r < M; ++r) nrm += cnorm2(w[s][r]);
+    const double in = 1.0 / sqrt(nrm);
+#pragma unroll
+    for (int r = 0; r < M; ++r) w[s][r] = cscale(w[s][r], in);
+  }
+  double tr = 0.0;   // Re Tr(W^H E)
+#pragma unroll
+  for (int s = 0; s < M; ++s)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      w_out[r * M + s] = w[s][r];
+      const double2 p = cmulc(w[s][r], e[r * M + s]);
+      tr += p.x;
+    }
+  return tr;
+}
+
+// Reference implementation with runtime sizes (kept for the host build's
+// cross-check of polar_jacobi_m); the kernels call polar_jacobi_m.
+QM_HD double polar_jacobi_ref(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
   double2 a[4][4], vv[4][4], u[4][4];
   for (int c = 0; c < m; ++c)
     for (int r = 0; r < m; ++r) a[c][r] = e[r * m + c];
@@ -447,4 +898,14 @@ QM_HD void ran_gate_single(const double2* v2, double2* g) {
     g[p * 2 + 0] = v2[p];
     g[p * 2 + 1] = b[p];
   }
+}
+
+// Polar factor dispatch (m in {2, 4}).
+QM_HD double polar_jacobi(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
+  return m == 4 ? polar_jacobi_m<4>(e, w_out, w_prev) : polar_jacobi_m<2>(e, w_out, w_prev);
+}
+
+// Polar factor used by the sweep kernel (FP32 sweeps, FP64 finish).
+QM_HD double polar_sweep(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
+  return m == 4 ? polar_fast<4>(e, w_out, w_prev) : polar_fast<2>(e, w_out, w_prev);
 }

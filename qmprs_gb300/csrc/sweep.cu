@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_polar(BatchDev bd, int 
         atomicOr(bd.err, KERR_NONFINITE);
       } else {
         for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
-        const double nn = polar_jacobi(env, m, w, wprev);
+        const double nn = polar_sweep(env, m, w, wprev);
         for (int i = 0; i < m * m; ++i) gptr[i] = cconj(w[i]);
         nuc[b] = nn;
       }

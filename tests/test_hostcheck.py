@@ -22,6 +22,8 @@ def hc():
     lib.hc_herm_eig.argtypes = [dp, ctypes.c_int, dp, dp]
     lib.hc_polar.argtypes = [dp, ctypes.c_int, dp, dp]
     lib.hc_polar.restype = ctypes.c_double
+    lib.hc_polar_sweep.argtypes = [dp, ctypes.c_int, dp, dp]
+    lib.hc_polar_sweep.restype = ctypes.c_double
     lib.hc_complement.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
     lib.hc_rank_by_cutoff.argtypes = [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.hc_rank_by_cutoff.restype = ctypes.c_int
@@ -107,6 +109,51 @@ def test_polar_null_space_follows_previous(hc, rank, seed):
     ref, _ = cv.polar_unitary_canonical(e, prev)
     assert np.allclose(w.conj().T @ w, np.eye(4), atol=1e-10)
     assert np.allclose(w, ref, atol=1e-7)
+
+
+@pytest.mark.parametrize("m", [2, 4])
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("cond", [1.0, 1e-3, 1e-5])
+def test_sweep_polar_fp32_sweeps(hc, m, seed, cond):
+    """The sweep kernel's polar (FP32 Jacobi, FP64 orthonormalisation and
+    trace): W is unitary to FP64 rounding, within FP32 accuracy of the exact
+    polar factor, and its trace Re Tr(W^H E) -- the fidelity the sweep
+    reports -- matches the nuclear norm to second order."""
+    rng = np.random.default_rng(100 + seed)
+    q1, _ = np.linalg.qr(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    q2, _ = np.linalg.qr(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    sv = np.geomspace(1.0, cond, m) * 0.37
+    e = _c(q1 @ np.diag(sv) @ q2)
+    w = np.zeros((m, m), np.complex128)
+    nuc = hc.hc_polar_sweep(_p(e), m, _p(w), None)
+    wref, s = cv.polar_unitary(e)
+    assert np.allclose(w.conj().T @ w, np.eye(m), atol=1e-14)
+    assert np.allclose(w, wref, atol=2e-5 / max(cond, 1e-2))
+    # error ~ s_min * (eps32 / cond)^2: 1e-11 relative at cond 1e-5
+    assert abs(nuc - s.sum()) <= 1e-10 * s.sum()
+
+
+@pytest.mark.parametrize("rank", [0, 1, 2, 3])
+@pytest.mark.parametrize("seed", range(3))
+def test_sweep_polar_null_space(hc, rank, seed):
+    """Rank-deficient environments in the sweep kernel's polar: same
+    completion as the oracle's canonical rule, to FP32 accuracy."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((4, rank)) + 1j * rng.standard_normal((4, rank))
+    b = rng.standard_normal((rank, 4)) + 1j * rng.standard_normal((rank, 4))
+    e = _c(a @ b)
+    e = e + 1e-9 * (rng.standard_normal((4, 4)))
+    prev, _ = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    prev = _c(prev)
+    w = np.zeros((4, 4), np.complex128)
+    nuc = hc.hc_polar_sweep(_p(_c(e)), 4, _p(w), _p(prev))
+    ref, s = cv.polar_unitary_canonical(e, prev)
+    assert np.allclose(w.conj().T @ w, np.eye(4), atol=1e-14)
+    assert np.allclose(w, ref, atol=1e-4)
+    sv = np.linalg.svd(e, compute_uv=False)
+    # the null directions (below 1e-6 s_max) are filled towards prev, so they
+    # contribute anything in [-s_null, s_null] to the trace
+    assert abs(nuc - sv[:rank].sum()) <= sv[rank:].sum() + 1e-10 * max(1.0, sv[0])
 
 
 @pytest.mark.parametrize("k,n", [(1, 2), (1, 4), (2, 4)])

@@ -15,10 +15,11 @@ sweeps -> circuit state -> fidelity) over the batch.
 * ``e2e``    the same through the public batched API
   (``Sequential.prepare_states``) from pinned HOST buffers, with the
   host->device input copy and the device->host result copy timed.
-* ``roofline``  the environment-sweep kernel (k_sweep_env): algorithmic
-  bytes (24 B per amplitude of every active state: read psi, read t,
-  write psi) over its event-timed launches in a profiled pass of the same
-  batch, against the measured HBM copy bandwidth.
+* ``roofline``  the grouped sweep pass (k_group_pass): algorithmic bytes
+  (32 B per amplitude of every state the pass touches: read and write psi
+  and t; 16 B for a state's first group, which only reads) over its
+  event-timed launches in a profiled pass of the same batch, against the
+  measured HBM copy bandwidth.
 * ``cpu_baseline``  the FP64 oracle's call-by-call restatement of the
   reference (``oracle.mpsops``, literal conventions, one state per process,
   OPENBLAS_NUM_THREADS=1) on a bounded stratified sample; the per-state
@@ -48,11 +49,12 @@ if ROOT not in sys.path:
 
 METRIC = "states/sec to fidelity≥0.98: learned warm-start+batched vs plain sweep, 1 GB300"
 UNIT = "states/s"
-# DRAM bytes (read + write) per amplitude of one k_sweep_env launch, from an
-# ncu capture of `python -m qmprs_gb300.profile_workload --states 32 --sweeps 1`
-# (dram__bytes_read.sum + dram__bytes_write.sum = 521.0 MB over 23,195,648
-# amplitudes); the full-size launch is scaled by its amplitude count.
-ENV_DRAM_BYTES_PER_AMP = 521.0e6 / 23195648
+# DRAM bytes (read + write) per algorithmic byte of a k_group_pass launch,
+# from an ncu capture of `python -m qmprs_gb300.profile_workload --states 32
+# --sweeps 1` (a group-1 launch: dram__bytes_read.sum + dram__bytes_write.sum
+# = 371.3 + 312.7 MB against 32 B x 23,195,648 amplitudes); a full-size
+# launch is scaled by its algorithmic bytes.
+PASS_DRAM_PER_ALG_BYTE = (371.317504e6 + 312.748544e6) / (32.0 * 23195648)
 
 
 def workload_spec(name: str, states: int, seed: int):
@@ -322,14 +324,14 @@ def run_gpu(args, rank, world):
                    "l2": f"inputs larger than L2 ({vec_gb:.1f} GB of statevectors per copy)",
                    "reached_0.98": reached, "mean_fidelity": float(np.mean(fid)),
                    "mean_sweeps_run": float(np.mean(sd))},
-        "roofline": {"bound": "hbm", "kernel": "k_sweep_env", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "k_group_pass", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ENV_DRAM_BYTES_PER_AMP * (by_env / max(n_env, 1)) / 24.0,
-                     "traffic_note": "DRAM bytes per launch, scaled by amplitudes from a 32-state ncu capture",
+                     "traffic": PASS_DRAM_PER_ALG_BYTE * (by_env / max(n_env, 1)),
+                     "traffic_note": "DRAM bytes per launch, scaled by algorithmic bytes from a 32-state ncu capture",
                      "launches": n_env, "avg_launch_us": ms_env / max(n_env, 1) * 1e3,
                      "bytes_per_launch": by_env / max(n_env, 1),
-                     "sweep_kernel_ms": {"env_stream": prof[0][1], "env_polar": prof[3][1],
-                                         "target_update": prof[1][1], "rebuild": prof[2][1]}},
+                     "sweep_kernel_ms": {"group_pass": prof[0][1], "group_polar": prof[3][1],
+                                         "rebuild": prof[2][1]}},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "5 states of the workload family with 12-14 qubits, one per core, "
                                    "oracle restatement of the reference (literal conventions); per-state "

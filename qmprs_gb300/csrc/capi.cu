@@ -42,6 +42,13 @@ struct qmprs_plan {
   double* nuc = nullptr;
   double2 *sq = nullptr, *tnorm = nullptr;
   BatchDev bd;
+  // grouped sweep: chunk tables, group plan, replaced gates, chunk partials
+  int nchunks = 0;
+  int *d_chunk_state = nullptr, *d_chunk_idx = nullptr, *d_state_chunk0 = nullptr, *d_state_nchunks = nullptr,
+      *d_ngroups = nullptr;
+  GroupEnt* d_grp = nullptr;
+  double2 *d_old_gates = nullptr, *d_gpartials = nullptr;
+  GroupDev gd;
   // profiling of the sweep kernels (kernel classes: 0 environment stream,
   // 1 target update, 2 circuit rebuild, 3 environment reduce + polar):
   // launches, event time, algorithmic bytes
@@ -227,7 +234,8 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->d_bond_init, p->S0,        p->S1,         p->S2,            p->partials,
                   p->tt_partials, p->gram,      p->vsel,       p->vsel2,         p->site_t, p->vwork,
                   p->bonds,    p->active,       p->nlayers,    p->num_active,    p->nuc,
-                  p->sq,       p->tnorm};
+                  p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
+                  p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -281,6 +289,20 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
     }
   }
   p->ntiles = (int)tile_state.size();
+  // grouped sweep: tiles of 2^min(n, GT) amplitudes, GCHUNK tiles per chunk
+  std::vector<int> chunk_state, chunk_idx, state_chunk0(num_states), state_nchunks(num_states);
+  for (int b = 0; b < num_states; ++b) {
+    const int n = p->n[b];
+    const int64_t tiles = n > GT ? ipow2(n - GT) : 1;
+    const int nc = (int)((tiles + GCHUNK - 1) / GCHUNK);
+    state_chunk0[b] = (int)chunk_state.size();
+    state_nchunks[b] = nc;
+    for (int c = 0; c < nc; ++c) {
+      chunk_state.push_back(b);
+      chunk_idx.push_back(c);
+    }
+  }
+  p->nchunks = (int)chunk_state.size();
   std::vector<int> bond_init((size_t)num_states * (p->max_n + 1), 0);
   for (int b = 0; b < num_states; ++b) {
     bond_init[(size_t)b * (p->max_n + 1)] = 1;
@@ -331,7 +353,32 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   PC(dalloc(&p->nuc, B));
   PC(dalloc(&p->sq, B));
   PC(dalloc(&p->tnorm, B));
+  const int gmax = max_layers * p->max_n;
+  PC(dalloc(&p->d_chunk_state, p->nchunks));
+  PC(dalloc(&p->d_chunk_idx, p->nchunks));
+  PC(dalloc(&p->d_state_chunk0, B));
+  PC(dalloc(&p->d_state_nchunks, B));
+  PC(dalloc(&p->d_ngroups, B));
+  PC(dalloc(&p->d_grp, (int64_t)B * gmax));
+  PC(dalloc(&p->d_old_gates, (int64_t)B * GMAXSTEPS * 16));
+  PC(dalloc(&p->d_gpartials, (int64_t)p->nchunks * GMM));
+  PC(cudaMemcpy(p->d_chunk_state, chunk_state.data(), sizeof(int) * p->nchunks, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_chunk_idx, chunk_idx.data(), sizeof(int) * p->nchunks, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_state_chunk0, state_chunk0.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemcpy(p->d_state_nchunks, state_nchunks.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  PC(cudaMemset(p->d_gpartials, 0, sizeof(double2) * (size_t)p->nchunks * GMM));
 #undef PC
+  GroupDev& gd = p->gd;
+  gd.nchunks = p->nchunks;
+  gd.gmax = gmax;
+  gd.chunk_state = p->d_chunk_state;
+  gd.chunk_idx = p->d_chunk_idx;
+  gd.state_chunk0 = p->d_state_chunk0;
+  gd.state_nchunks = p->d_state_nchunks;
+  gd.grp = p->d_grp;
+  gd.ngroups = p->d_ngroups;
+  gd.old_gates = p->d_old_gates;
+  gd.partials = p->d_gpartials;
   BatchDev& bd = p->bd;
   bd.B = B;
   bd.ntiles = p->ntiles;
@@ -487,20 +534,31 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   if (rc != QMPRS_OK) return rc;
   launch_fill_int(p->active, p->B, 1, s);
   launch_overlap(p->bd, target, target, p->partials, p->tnorm, s);
+  // group plan of the backward order (the gates' arity does not change
+  // between sweeps)
+  launch_group_plan(p->bd, p->gd, ar, num_layers, s);
+  std::vector<int> ngroups(p->B, 0);
+  CK(cudaMemcpyAsync(ngroups.data(), p->d_ngroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int max_groups = 0;
+  for (int b = 0; b < p->B; ++b) max_groups = std::max(max_groups, ngroups[b]);
   float2* psi = p->S0;
   float2* t = p->S1;
   ProfLog log;
   const bool prof = p->prof;
   std::vector<int> act(p->B, 1);
   for (int sw = 0; sw < num_sweeps; ++sw) {
-    // algorithmic bytes per step j, counted from the states active in this sweep
-    std::vector<double> amp_at(prof ? max_gates : 0, 0.0);
+    // algorithmic bytes per rebuild pass / group pass, counted from the
+    // states active in this sweep
+    std::vector<double> amp_at(prof ? max_gates : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
     if (prof) {
       CK(cudaMemcpyAsync(act.data(), p->active, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       for (int b = 0; b < p->B; ++b)
-        if (act[b])
+        if (act[b]) {
           for (int j = 0; j < p->gates_per_state[b]; ++j) amp_at[j] += (double)ipow2(p->n[b]);
+          for (int g = 0; g < ngroups[b]; ++g) amp_grp[g] += (double)ipow2(p->n[b]);
+        }
     }
     // C|0>: three consecutive gates per pass on 4-qubit windows
     launch_set_zero_state(p->bd, psi, p->active, s);
@@ -510,17 +568,19 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
       log.end(prof, 2, s);
       if (prof) p->prof_bytes[2] += 16.0 * amp_at[j];
     }
-    CK(cudaMemcpyAsync(t, target, sizeof(float2) * p->vec_total, cudaMemcpyDeviceToDevice, s));
-    // backward sweep: step j peels gate j off psi, applies step j-1's new gate
-    // to t and reduces E_j; the polar kernel turns E_j into the new gate
-    for (int j = 0; j < max_gates; ++j) {
+    // backward sweep by groups: the pass applies group g-1's peels to psi
+    // and its new gates to t (the target itself for g = 1) and reduces the
+    // cross matrix of group g; the polar kernel runs group g's steps on it
+    for (int g = 0; g < max_groups; ++g) {
       log.begin(prof, s);
-      launch_env_win(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, s);
+      const int e = launch_group_pass(p->bd, p->gd, g, psi, g <= 1 ? target : t, t, gates, ar, num_layers,
+                                      p->active, s);
+      if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "cudaFuncSetAttribute(k_group_pass)");
       log.end(prof, 0, s);
       log.begin(prof, s);
-      launch_sweep_polar(p->bd, j, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
+      launch_group_polar(p->bd, p->gd, g, gates, ar, num_layers, p->active, p->nuc, s);
       log.end(prof, 3, s);
-      if (prof) p->prof_bytes[0] += (j == 0 ? 24.0 : 32.0) * amp_at[j];
+      if (prof) p->prof_bytes[0] += (g == 0 ? 16.0 : 32.0) * amp_grp[g];
     }
     log.flush(p);
     CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));

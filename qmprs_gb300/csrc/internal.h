@@ -90,6 +90,37 @@ struct GateSel {
   const int* active;    // [B] state participates (may be null)
 };
 
+// Grouped backward sweep (sweep_group.cu): a group is a run of consecutive
+// backward steps whose qubits fit a window of GW qubits; one pass over the
+// vectors per group, shared-memory tiles of 2^GT amplitudes, one partial
+// cross matrix per chunk of GCHUNK tiles.
+#define GW 4
+#define GM (1 << GW)
+#define GMM (GM * GM)
+#define GT 12
+#define GCHUNK 16
+#define GMAXSTEPS 8
+
+struct GroupEnt {
+  int j0;     // first backward step
+  int cnt;    // steps in the group
+  int qmask;  // window qubits (bit q = qubit q), exactly u of them
+  int u;      // window size min(GW, n)
+};
+
+struct GroupDev {
+  int nchunks;
+  int gmax;                  // group slots per state (max_layers * max_n)
+  const int* chunk_state;    // [nchunks]
+  const int* chunk_idx;      // [nchunks] chunk index within its state
+  const int* state_chunk0;   // [B]
+  const int* state_nchunks;  // [B]
+  GroupEnt* grp;             // [B * gmax]
+  int* ngroups;              // [B]
+  double2* old_gates;        // [B * GMAXSTEPS * 16] gates replaced by the last group
+  double2* partials;         // [nchunks * GMM]
+};
+
 // ---- launches (defined in the .cu files) ---------------------------------
 void launch_set_zero_state(const BatchDev& bd, float2* vec, const int* active, cudaStream_t s);
 void launch_apply_gate(const BatchDev& bd, float2* vec, const GateSel& sel, cudaStream_t s);
@@ -113,17 +144,15 @@ void launch_layer_fidelity(const BatchDev& bd, int layer, const float2* work, in
                            cudaStream_t s);
 
 // (d) sweep
-void launch_sweep_env(const BatchDev& bd, int step, float2* psi, const float2* t,
-                      double2* gates, const signed char* arity, const int* nlayers,
-                      const int* active, double2* partials, double* nuc, cudaStream_t s);
 void launch_rebuild_win(const BatchDev& bd, float2* psi, const double2* gates, const signed char* arity,
                         const int* nlayers, const int* active, int j0, int count, cudaStream_t s);
-void launch_env_win(const BatchDev& bd, int step, float2* psi, float2* t, const double2* gates,
-                    const signed char* arity, const int* nlayers, const int* active, double2* partials,
-                    cudaStream_t s);
-void launch_sweep_polar(const BatchDev& bd, int step, double2* gates, const signed char* arity,
-                        const int* nlayers, const int* active, const double2* partials, double* nuc,
-                        cudaStream_t s);
+void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, const int* nlayers,
+                       cudaStream_t s);
+int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
+                      const double2* gates, const signed char* arity, const int* nlayers, const int* active,
+                      cudaStream_t s);
+void launch_group_polar(const BatchDev& bd, const GroupDev& gd, int g, double2* gates, const signed char* arity,
+                        const int* nlayers, const int* active, double* nuc, cudaStream_t s);
 void launch_sweep_finish(int B, int sweep, int num_sweeps, const double* nuc, const double2* tnorm2,
                          double* sweep_fid, int* sweeps_done, int* active, double stop_fid,
                          int* num_active, cudaStream_t s);

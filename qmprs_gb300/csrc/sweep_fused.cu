@@ -1,33 +1,13 @@
-// Fused sweep passes on qubit windows (the production sweep of
-// qmprs_optimize_layers).
+// Circuit rebuild of the sweep (reference
+// qmprs/synthesis/mps_encoding/sequential.py:443-447 densifies C|0> at the
+// start of every sweep).
 //
 // k_rebuild_win  builds C|0> applying up to three consecutive gates of every
 //                state per pass: three consecutive gates of the circuit order
 //                touch at most four qubits, so a thread holds the 16
 //                amplitudes of one 4-qubit window and applies them in
 //                registers.  16 B of HBM traffic per amplitude per pass.
-// k_env_win      one gate step of the backward sweep (reference
-//                qmprs/synthesis/mps_encoding/sequential.py:452-505) fused
-//                with the target update of the previous step: on a 3-qubit
-//                window it applies the previous step's new gate (adjoint) to t
-//                (:496), peels the current gate off psi (:460) and
-//                accumulates the environment E (:463).  Consecutive steps of
-//                the backward order touch at most three qubits.  32 B per
-//                amplitude (read and write psi and t) instead of 24 + 16 for
-//                separate passes.
-// The polar update of each step stays in k_sweep_polar (sweep.cu).
 #include "window.cuh"
-
-// Gate of state b at backward sweep step j (circuit gate G-1-j): slot, site, arity.
-__device__ __forceinline__ bool sweep_gate(const BatchDev& bd, const signed char* arity, int L, int n, int b,
-                                           int j, int64_t* slot, int* q, int* k) {
-  if (j < 0 || j >= L * n) return false;
-  const int l = j / n, s = n - 1 - j % n;
-  *slot = (int64_t)l * n + s;
-  *q = s;
-  *k = arity[bd.gate_off[b] / 16 + *slot];
-  return (*k == 1) || (*k == 2 && s <= n - 2);
-}
 
 // Gate of state b at forward position j (circuit order): generated layer L-1-j/n, site j%n.
 __device__ __forceinline__ bool fwd_gate(const BatchDev& bd, const signed char* arity, int L, int n, int b, int j,
@@ -111,78 +91,6 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 2) k_rebuild_win(BatchDev bd, f
   }
 }
 
-template <int U>
-__device__ __forceinline__ void env_groups(const BatchDev& bd, int b, int n, int tile, float2* v, float2* tv,
-                                           const WinSpec& w, const float2* gcur, int kc, int hc, int lc,
-                                           const float2* gpend, int kp, int hp, int lp, bool pending,
-                                           double2* partials) {
-  int off[1 << U];
-  win_offsets<U>(w, off);
-  int64_t lo, hi;
-  tile_range(ipow2(n - U), bd.tile_idx[tile], bd.state_ntiles[b], &lo, &hi);
-  float2 e[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) e[i] = cf(0.f, 0.f);
-  for (int64_t r = lo + threadIdx.x; r < hi; r += blockDim.x) {
-    const int64_t base = win_base(w, r);
-    float2 x[1 << U], z[1 << U];
-#pragma unroll
-    for (int li = 0; li < (1 << U); ++li) {
-      x[li] = v[base + off[li]];
-      z[li] = tv[base + off[li]];
-    }
-    if (pending) {
-      win_apply<U>(z, gpend, kp, hp, lp);
-#pragma unroll
-      for (int li = 0; li < (1 << U); ++li) tv[base + off[li]] = z[li];
-    }
-    win_apply<U>(x, gcur, kc, hc, lc);
-#pragma unroll
-    for (int li = 0; li < (1 << U); ++li) v[base + off[li]] = x[li];
-    win_env<U>(z, x, e, kc, hc, lc);
-  }
-  warp_partial16(e, partials + ((int64_t)tile * WARPS + (threadIdx.x >> 5)) * 16);
-}
-
-__global__ void __launch_bounds__(BLOCK_THREADS, 2) k_env_win(BatchDev bd, int step, float2* psi, float2* t,
-                                                           const double2* gates, const signed char* arity,
-                                                           const int* nlayers, const int* active,
-                                                           double2* partials) {
-  __shared__ float2 gcur[16], gpend[16];
-  for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
-    const int b = bd.tile_state[tile];
-    if (active && !active[b]) continue;
-    const int n = bd.n[b];
-    const int L = nlayers[b];
-    int64_t sc, sp;
-    int qc, kc, qp, kp;
-    if (!sweep_gate(bd, arity, L, n, b, step, &sc, &qc, &kc)) continue;
-    const bool pending = sweep_gate(bd, arity, L, n, b, step - 1, &sp, &qp, &kp);
-    int qs[4], nq = 0;
-    qs[nq++] = qc;
-    if (kc == 2) qs[nq++] = qc + 1;
-    if (pending) {
-      qs[nq++] = qp;
-      if (kp == 2) qs[nq++] = qp + 1;
-    }
-    WinSpec w;
-    if (!win_build(w, n, qs, nq, n < 3 ? n : 3)) {
-      if (threadIdx.x == 0) atomicOr(bd.err, KERR_BAD_GATE);
-      continue;
-    }
-    const int hc = win_local(w, qc), lc = kc == 2 ? win_local(w, qc + 1) : 0;
-    const int hp = pending ? win_local(w, qp) : 0, lp = (pending && kp == 2) ? win_local(w, qp + 1) : 0;
-    __syncthreads();
-    stage_gate(gcur, gates + bd.gate_off[b] + sc * 16, kc, 1);
-    if (pending) stage_gate(gpend, gates + bd.gate_off[b] + sp * 16, kp, 1);
-    __syncthreads();
-    float2* v = psi + bd.vec_off[b];
-    float2* tv = t + bd.vec_off[b];
-    if (w.u == 3) env_groups<3>(bd, b, n, tile, v, tv, w, gcur, kc, hc, lc, gpend, kp, hp, lp, pending, partials);
-    else env_groups<2>(bd, b, n, tile, v, tv, w, gcur, kc, hc, lc, gpend, kp, hp, lp, pending, partials);
-  }
-}
-
 static int grid_for(const BatchDev& bd) {
   int g = bd.ntiles;
   const int cap = 152 * 8;
@@ -193,11 +101,4 @@ void launch_rebuild_win(const BatchDev& bd, float2* psi, const double2* gates, c
                         const int* nlayers, const int* active, int j0, int count, cudaStream_t s) {
   qm_note_launch();
   k_rebuild_win<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, psi, gates, arity, nlayers, active, j0, count);
-}
-
-void launch_env_win(const BatchDev& bd, int step, float2* psi, float2* t, const double2* gates,
-                    const signed char* arity, const int* nlayers, const int* active, double2* partials,
-                    cudaStream_t s) {
-  qm_note_launch();
-  k_env_win<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, step, psi, t, gates, arity, nlayers, active, partials);
 }

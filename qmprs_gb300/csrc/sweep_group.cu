@@ -1,0 +1,719 @@
+// Grouped backward sweep: the production sweep of qmprs_optimize_layers.
+//
+// Restates the body of Sequential._sweep_unitary_layers (reference
+// qmprs/synthesis/mps_encoding/sequential.py:452-505) on dense vectors.  Per
+// gate of the backward order:
+//   psi <- G^H psi                                    (:460)
+//   E[a][b] = sum_rest conj(t[a, rest]) psi[b, rest]  (:463)
+//   new gate = conj(W), W = u @ vh of E               (:473-478, :501-505)
+//   t <- new^H t                                      (:496)
+//
+// Consecutive steps of the backward order touch neighbouring qubits.  A
+// group is a run of consecutive steps whose qubits fit a window of
+// u = min(GW, n) qubits.  With x the circuit-side vector and z the
+// target-side vector, both read as 2^u x rest matrices over the window, the
+// cross matrix
+//   M[i][k] = sum_rest conj(z[i, rest]) x[k, rest]
+// carries every environment of the group: x <- Q x maps M to M Q^T,
+// z <- P z maps M to conj(P) M, and the environment of a gate on window
+// bits (h, l) is the partial trace E[r][c] = sum_o M[(r, o)][(c, o)].
+// A group therefore costs one pass over the vectors and one small kernel:
+//   k_group_pass   shared-memory tiles of 2^GT amplitudes: apply the
+//                  previous group's peels to x and its new gates to z,
+//                  write both back, and reduce this group's M (fp32 per
+//                  thread over a chunk of GCHUNK tiles, fp64 across the
+//                  block, one partial per chunk)
+//   k_group_polar  one block per state: sum the chunk partials in chunk
+//                  order, then run the group's steps on M in fp64 (target
+//                  update, peel, partial trace, polar factor), keeping the
+//                  replaced gates for the next pass
+// Group 0 only reads (x = C|0>, z = the target); group 1 reads the target
+// and writes t, so the target is never copied.  After the last group the
+// vectors are not needed: the sweep's fidelity is the last step's trace.
+#include "window.cuh"
+
+// Gate of state b at backward step j: generated layer j / n, site
+// n - 1 - j % n.
+__device__ __forceinline__ bool bwd_step(const BatchDev& bd, const signed char* arity, int L, int n, int b, int j,
+                                         int64_t* slot, int* q, int* k) {
+  if (j < 0 || j >= L * n) return false;
+  const int l = j / n, s = n - 1 - j % n;
+  *slot = (int64_t)l * n + s;
+  *q = s;
+  *k = arity[bd.gate_off[b] / 16 + *slot];
+  return (*k == 1) || (*k == 2 && s <= n - 2);
+}
+
+// Place the low bits of v, in order, at the set bits of mask (ascending).
+__device__ __forceinline__ int64_t deposit_bits(int64_t v, int64_t mask) {
+  int64_t r = 0;
+  while (mask) {
+    const int64_t bit = mask & (-mask);
+    if (v & 1) r |= bit;
+    v >>= 1;
+    mask ^= bit;
+  }
+  return r;
+}
+
+// Shared-memory swizzle of a tile index: the low four bits (the float2
+// slot within a 128-byte bank row) are XORed with bits 4-7 and 8-11, so
+// that warps walking low, middle or high tile bits hit distinct banks.  The
+// map is linear over XOR, so for disjoint bit sets swz(a | b) =
+// swz(a) ^ swz(b) and the offset tables below hold swizzled values.
+__device__ __forceinline__ int swz(int li) { return li ^ (((li >> 4) ^ (li >> 8)) & 15); }
+
+// (a.x * b.x + c.x, a.y * b.y + c.y) as one packed FP32 FMA.
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// ---- group plan --------------------------------------------------------------
+
+__global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bd.B; b += gridDim.x * blockDim.x) {
+    const int n = bd.n[b], L = nlayers[b], total = L * n;
+    const int u = n < GW ? n : GW;
+    int ng = 0, j = 0;
+    while (j < total) {
+      int64_t slot;
+      int q, k;
+      if (!bwd_step(bd, arity, L, n, b, j, &slot, &q, &k)) {
+        atomicOr(bd.err, KERR_BAD_GATE);   // skipped, as the per-gate launches do
+        ++j;
+        continue;
+      }
+      int mask = (k == 2 ? 3 : 1) << q;
+      const int j0 = j++;
+      while (j < total && j - j0 < GMAXSTEPS) {
+        if (!bwd_step(bd, arity, L, n, b, j, &slot, &q, &k)) break;
+        const int m2 = mask | ((k == 2 ? 3 : 1) << q);
+        if (__popc(m2) > u) break;
+        mask = m2;
+        ++j;
+      }
+      for (int qq = n - 1; qq >= 0 && __popc(mask) < u; --qq) mask |= 1 << qq;
+      if (ng < gd.gmax) {
+        GroupEnt e;
+        e.j0 = j0;
+        e.cnt = j - j0;
+        e.qmask = mask;
+        e.u = u;
+        gd.grp[(int64_t)b * gd.gmax + ng] = e;
+        ++ng;
+      }
+    }
+    gd.ngroups[b] = ng;
+  }
+}
+
+// ---- pass kernel ---------------------------------------------------------------
+
+struct PassShared {
+  int pos_mask;             // global bit positions held in the tile
+  int T;                    // tile bits
+  int wml_c, wml_p;         // tile-local bit masks of the current / previous window
+  int npk;                  // previous group's steps
+  int pk[GMAXSTEPS], phi[GMAXSTEPS], plo[GMAXSTEPS];
+  int wl[GM], wlp[GM];      // window index -> swizzled tile offset
+  int rl[1 << (GT - GW)];   // rest index -> swizzled tile offset (current window)
+  int plp[1 << (GT - GW)];  // rest index -> swizzled tile offset (previous window)
+  int d0[64], d1[64];       // global offset of tile index li: d0[li & 63] | d1[li >> 6]
+  float2 gr[2][GMAXSTEPS][16];   // [peel | new][step]: (re, re) of the applied matrix
+  float2 gi[2][GMAXSTEPS][16];   // (im, im)
+};
+
+// Dynamic shared memory: two tile buffers (x and z, float2 each) and the
+// target side of the current tile duplicated as (re, re, im, im) for the
+// cross reduction.
+#define PASS_DYN_SMEM ((size_t)(4 * sizeof(float2) + sizeof(float4)) * (1 << GT))
+
+// tile-local bit of global position p (p must be in pos_mask)
+__device__ __forceinline__ int tile_bit(int pos_mask, int p) { return __popc(pos_mask & ((1 << p) - 1)); }
+
+__device__ __forceinline__ int deposit32(int v, int mask) {
+  int r = 0;
+  while (mask) {
+    const int bit = mask & (-mask);
+    if (v & 1) r |= bit;
+    v >>= 1;
+    mask ^= bit;
+  }
+  return r;
+}
+
+// y = G x on window bits (H, L), G given as gr[i] = (re, re), gi[i] = (im, im):
+// two packed accumulators pa = sum (gr xr, gr xi), pb = sum (gi xr, gi xi),
+// y = (pa.x - pb.y, pa.y + pb.x).  No operand needs a swap or a negation.
+template <int U, int H, int L>
+__device__ __forceinline__ void apply2_p(float2 (&a)[1 << U], const float2* gr, const float2* gi) {
+#pragma unroll
+  for (int o = 0; o < (1 << (U - 2)); ++o) {
+    const int b = win_other2<U, H, L>(o);
+    const int idx[4] = {b, b | (1 << L), b | (1 << H), b | (1 << H) | (1 << L)};
+    float2 x[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c] = a[idx[c]];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float2 pa = cf(0.f, 0.f), pb = cf(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        pa = f2fma(gr[r * 4 + c], x[c], pa);
+        pb = f2fma(gi[r * 4 + c], x[c], pb);
+      }
+      a[idx[r]] = cf(pa.x - pb.y, pa.y + pb.x);
+    }
+  }
+}
+
+template <int U, int B>
+__device__ __forceinline__ void apply1_p(float2 (&a)[1 << U], const float2* gr, const float2* gi) {
+#pragma unroll
+  for (int o = 0; o < (1 << (U - 1)); ++o) {
+    const int b = win_other1<U, B>(o);
+    const float2 x0 = a[b], x1 = a[b | (1 << B)];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      float2 pa = f2fma(gr[r * 2 + 1], x1, f2fma(gr[r * 2], x0, cf(0.f, 0.f)));
+      float2 pb = f2fma(gi[r * 2 + 1], x1, f2fma(gi[r * 2], x0, cf(0.f, 0.f)));
+      a[r ? (b | (1 << B)) : b] = cf(pa.x - pb.y, pa.y + pb.x);
+    }
+  }
+}
+
+template <int U>
+__device__ __forceinline__ void apply_p(float2 (&a)[1 << U], const float2* gr, const float2* gi, int k, int hi,
+                                        int lo) {
+  if (k == 2) {
+    if (U == 2) {
+      apply2_p<U, 1, 0>(a, gr, gi);
+    } else if (U == 3) {
+      if (hi == 2 && lo == 1) apply2_p<U, 2, 1>(a, gr, gi);
+      else if (hi == 1 && lo == 0) apply2_p<U, 1, 0>(a, gr, gi);
+      else apply2_p<U, 2, 0>(a, gr, gi);
+    } else {
+      switch (hi * 4 + lo) {
+        case 3 * 4 + 2: apply2_p<U, 3, 2>(a, gr, gi); break;
+        case 3 * 4 + 1: apply2_p<U, 3, 1>(a, gr, gi); break;
+        case 3 * 4 + 0: apply2_p<U, 3, 0>(a, gr, gi); break;
+        case 2 * 4 + 1: apply2_p<U, 2, 1>(a, gr, gi); break;
+        case 2 * 4 + 0: apply2_p<U, 2, 0>(a, gr, gi); break;
+        default: apply2_p<U, 1, 0>(a, gr, gi); break;
+      }
+    }
+  } else {
+    switch (hi) {
+      case 0: apply1_p<U, 0>(a, gr, gi); break;
+      case 1: apply1_p<U, 1>(a, gr, gi); break;
+      case 2: if (U > 2) apply1_p<U, (U > 2 ? 2 : 0)>(a, gr, gi); break;
+      default: if (U > 3) apply1_p<U, (U > 3 ? 3 : 0)>(a, gr, gi); break;
+    }
+  }
+}
+
+// Previous group's peels on x and new gates on z, over the previous
+// window; z is also written duplicated into zd for the cross reduction.
+// With no previous group (g = 0) the tables describe the current window
+// and only the duplicate is written.
+template <int U>
+__device__ __forceinline__ void pass_apply(const PassShared& sh, float2* xs, float2* zs, float4* zd, bool prev) {
+  const int npos = 1 << (sh.T - U);
+  for (int p = threadIdx.x; p < npos; p += blockDim.x) {
+    const int po = sh.plp[p];
+    float2 a[1 << U];
+    if (prev) {
+#pragma unroll
+      for (int w = 0; w < (1 << U); ++w) a[w] = xs[po ^ sh.wlp[w]];
+      for (int s = 0; s < sh.npk; ++s)
+        if (sh.pk[s]) apply_p<U>(a, sh.gr[0][s], sh.gi[0][s], sh.pk[s], sh.phi[s], sh.plo[s]);
+#pragma unroll
+      for (int w = 0; w < (1 << U); ++w) xs[po ^ sh.wlp[w]] = a[w];
+    }
+#pragma unroll
+    for (int w = 0; w < (1 << U); ++w) a[w] = zs[po ^ sh.wlp[w]];
+    if (prev) {
+      for (int s = 0; s < sh.npk; ++s)
+        if (sh.pk[s]) apply_p<U>(a, sh.gr[1][s], sh.gi[1][s], sh.pk[s], sh.phi[s], sh.plo[s]);
+    }
+#pragma unroll
+    for (int w = 0; w < (1 << U); ++w) {
+      const int li = po ^ sh.wlp[w];
+      if (prev) zs[li] = a[w];
+      zd[li] = make_float4(a[w].x, a[w].x, a[w].y, a[w].y);
+    }
+  }
+}
+
+// Cross reduction over this thread's rests for the 4 x 4 block (bi, bk):
+// aa[i * 4 + k] += (zr, zr) * x_k, bb[i * 4 + k] += (zi, zi) * x_k, so that
+// M = sum conj(z_i) x_k = (aa.x + bb.y, aa.y - bb.x).
+template <int U>
+__device__ __forceinline__ void pass_cross(const PassShared& sh, const float2* xs, const float4* zd,
+                                           float2 (&aa)[16], float2 (&bb)[16]) {
+  constexpr int D = 1 << U, NBK = D / 4, NB = NBK * NBK;
+  const int blk = threadIdx.x % NB, rg = threadIdx.x / NB, nrg = blockDim.x / NB;
+  const int bi = blk / NBK, bk = blk % NBK;
+  const int nrest = 1 << (sh.T - U);
+  int wz[4], wx[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    wz[i] = sh.wl[4 * bi + i];
+    wx[i] = sh.wl[4 * bk + i];
+  }
+  for (int r = rg; r < nrest; r += nrg) {
+    const int ro = sh.rl[r];
+    float4 zv[4];
+    float2 xx[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      zv[i] = zd[wz[i] ^ ro];
+      xx[i] = xs[wx[i] ^ ro];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 zr = cf(zv[i].x, zv[i].y), zi = cf(zv[i].z, zv[i].w);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        aa[i * 4 + k] = f2fma(zr, xx[k], aa[i * 4 + k]);
+        bb[i * 4 + k] = f2fma(zi, xx[k], bb[i * 4 + k]);
+      }
+    }
+  }
+}
+
+// Sum the accumulators over the block's rest groups (fixed order) into the
+// chunk's partial (row-major 16 x 16 entries of M).  `red` aliases the tile
+// buffers.
+template <int U>
+__device__ __forceinline__ void pass_flush(const float2 (&aa)[16], const float2 (&bb)[16], double2* red,
+                                           double2* out) {
+  constexpr int D = 1 << U, NBK = D / 4, NB = NBK * NBK;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int blk = threadIdx.x % NB;
+  __syncthreads();   // tile buffers free
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    double re = (double)aa[e].x + (double)bb[e].y, im = (double)aa[e].y - (double)bb[e].x;
+#pragma unroll
+    for (int o = NB; o < 32; o <<= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane < NB) red[(warp * NB + blk) * 16 + e] = cd(re, im);
+  }
+  __syncthreads();
+  for (int ent = threadIdx.x; ent < NB * 16; ent += blockDim.x) {
+    double2 s = czero();
+    for (int w = 0; w < nwarps; ++w) s = cadd(s, red[(w * NB) * 16 + ent]);
+    const int b = ent / 16, e = ent % 16;
+    const int i = 4 * (b / NBK) + e / 4, k = 4 * (b % NBK) + e % 4;
+    out[i * GM + k] = s;
+  }
+  __syncthreads();
+}
+
+// Tile loads: 8-byte cp.async copies straight into swizzled shared memory,
+// one commit group per tile, so the next tile streams in while the current
+// one is processed.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Full tiles (2^GT amplitudes, BLOCK_THREADS threads): thread t handles
+// tile indices li = t + 256 u, whose offset is d0[t & 63] | d1[(t >> 6) + 4 u]
+// and whose swizzle is li ^ (((t >> 4) ^ u) & 15).
+#define PASS_PER ((1 << GT) / BLOCK_THREADS)
+static_assert(BLOCK_THREADS == 256 && GT == 12, "the full-tile index split assumes 256 threads and 2^12 tiles");
+
+__device__ __forceinline__ void pass_issue(const PassShared& sh, const float2* xg, const float2* zg, float2* xs,
+                                           float2* zs) {
+  if (sh.T == GT) {
+    const int t = threadIdx.x, lo = sh.d0[t & 63];
+#pragma unroll
+    for (int u = 0; u < PASS_PER; ++u) {
+      const int li = t + u * BLOCK_THREADS;
+      const int o = lo | sh.d1[(t >> 6) + 4 * u];
+      const int sl = li ^ (((t >> 4) ^ u) & 15);
+      cp_async8(xs + sl, xg + o);
+      cp_async8(zs + sl, zg + o);
+    }
+  } else {
+    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x) {
+      const int o = sh.d0[li & 63] | sh.d1[li >> 6];
+      cp_async8(xs + swz(li), xg + o);
+      cp_async8(zs + swz(li), zg + o);
+    }
+  }
+}
+
+__device__ __forceinline__ void pass_store(const PassShared& sh, float2* xg, float2* zg, const float2* xs,
+                                           const float2* zs) {
+  if (sh.T == GT) {
+    const int t = threadIdx.x, lo = sh.d0[t & 63];
+#pragma unroll
+    for (int u = 0; u < PASS_PER; ++u) {
+      const int li = t + u * BLOCK_THREADS;
+      const int o = lo | sh.d1[(t >> 6) + 4 * u];
+      const int sl = li ^ (((t >> 4) ^ u) & 15);
+      xg[o] = xs[sl];
+      zg[o] = zs[sl];
+    }
+  } else {
+    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x) {
+      const int o = sh.d0[li & 63] | sh.d1[li >> 6];
+      xg[o] = xs[swz(li)];
+      zg[o] = zs[swz(li)];
+    }
+  }
+}
+
+// next value with the same bits outside `mask` clear: the bits of `mask`
+// read as a counter
+__device__ __forceinline__ int64_t next_in_mask(int64_t x, int64_t mask) { return ((x | ~mask) + 1) & mask; }
+
+template <int U>
+__device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& gd, const PassShared& sh, float2* xs,
+                                           float4* zd, int g, int b, int chunk, float2* psi, const float2* z_in,
+                                           float2* z_out) {
+  const int n = bd.n[b];
+  const int64_t ntiles = (int64_t)1 << (n - sh.T);
+  const int64_t rest_mask = (((int64_t)1 << n) - 1) & ~(int64_t)sh.pos_mask;
+  float2* xv = psi + bd.vec_off[b];
+  const float2* zv_in = z_in + bd.vec_off[b];
+  float2* zv_out = z_out + bd.vec_off[b];
+  float2 aa[16], bb[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) aa[e] = bb[e] = cf(0.f, 0.f);
+  const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
+  const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
+  const int tsz = 1 << GT;   // buffer stride (tiles of small states use a prefix)
+  int64_t base = deposit_bits(t0, rest_mask);
+  pass_issue(sh, xv + base, zv_in + base, xs, xs + tsz);
+  cp_async_commit();
+  for (int64_t tt = t0; tt < t1; ++tt) {
+    const int cur = (int)((tt - t0) & 1);
+    float2* xb = xs + cur * 2 * tsz;
+    float2* zb = xb + tsz;
+    const int64_t nbase = next_in_mask(base, rest_mask);
+    if (tt + 1 < t1) {
+      float2* xn = xs + (cur ^ 1) * 2 * tsz;
+      pass_issue(sh, xv + nbase, zv_in + nbase, xn, xn + tsz);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    pass_apply<U>(sh, xb, zb, zd, g > 0);
+    __syncthreads();
+    if (g > 0) pass_store(sh, xv + base, zv_out + base, xb, zb);
+    pass_cross<U>(sh, xb, zd, aa, bb);
+    __syncthreads();
+    base = nbase;
+  }
+  cp_async_wait<0>();
+  pass_flush<U>(aa, bb, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
+}
+
+__global__ void __launch_bounds__(BLOCK_THREADS, 1) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
+                                                              const float2* z_in, float2* z_out,
+                                                              const double2* gates, const double2* old_gates,
+                                                              const signed char* arity, const int* nlayers,
+                                                              const int* active) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  float2* xs = reinterpret_cast<float2*>(dyn);   // buffer k: x at xs + 2k 2^GT, z right after
+  float4* zd = reinterpret_cast<float4*>(xs + 4 * (1 << GT));
+  __shared__ PassShared sh;
+  for (int chunk = blockIdx.x; chunk < gd.nchunks; chunk += gridDim.x) {
+    const int b = gd.chunk_state[chunk];
+    if (active && !active[b]) continue;
+    if (g >= gd.ngroups[b]) continue;
+    const int n = bd.n[b];
+    const int L = nlayers[b];
+    const GroupEnt cur = gd.grp[(int64_t)b * gd.gmax + g];
+    const GroupEnt prv = g > 0 ? gd.grp[(int64_t)b * gd.gmax + g - 1] : cur;
+    const int T = n < GT ? n : GT;
+    const int U = cur.u;
+    __syncthreads();   // previous chunk done with the tables
+    // step data of the previous group, one thread per step; the plan only
+    // groups valid steps
+    if (g > 0 && threadIdx.x < prv.cnt && threadIdx.x < GMAXSTEPS) {
+      const int s = threadIdx.x;
+      int64_t slot;
+      int q, k;
+      if (bwd_step(bd, arity, L, n, b, prv.j0 + s, &slot, &q, &k)) {
+        sh.pk[s] = k;
+        sh.phi[s] = __popc(prv.qmask >> (q + 1));   // window qubits above q
+        sh.plo[s] = k == 2 ? __popc(prv.qmask >> (q + 2)) : 0;
+      } else {
+        sh.pk[s] = 0;   // never applied
+      }
+    }
+    if (threadIdx.x == 0) {
+      int pm = 0;
+      const int qm = cur.qmask | prv.qmask;
+      for (int q = 0; q < n; ++q)
+        if ((qm >> q) & 1) pm |= 1 << (n - 1 - q);
+      for (int p = 0; p < n && __popc(pm) < T; ++p) pm |= 1 << p;
+      int wc = 0, wp = 0;
+      for (int q = 0; q < n; ++q) {
+        if ((cur.qmask >> q) & 1) wc |= 1 << tile_bit(pm, n - 1 - q);
+        if ((prv.qmask >> q) & 1) wp |= 1 << tile_bit(pm, n - 1 - q);
+      }
+      sh.pos_mask = pm;
+      sh.T = T;
+      sh.wml_c = wc;
+      sh.wml_p = wp;   // the current window when g = 0
+      sh.npk = g > 0 ? (prv.cnt < GMAXSTEPS ? prv.cnt : GMAXSTEPS) : 0;
+    }
+    __syncthreads();
+    const int full = (1 << T) - 1;
+    {
+      // split of pos_mask into its lowest six bits and the rest
+      int lo6 = 0, m = sh.pos_mask;
+      for (int i = 0; i < 6 && m; ++i) {
+        lo6 |= m & (-m);
+        m &= m - 1;
+      }
+      for (int j = threadIdx.x; j < 64; j += blockDim.x) {
+        sh.d0[j] = deposit32(j, lo6);
+        sh.d1[j] = deposit32(j, m);
+      }
+    }
+    for (int a = threadIdx.x; a < (1 << U); a += blockDim.x) {
+      sh.wl[a] = swz(deposit32(a, sh.wml_c));
+      sh.wlp[a] = swz(deposit32(a, sh.wml_p));
+    }
+    for (int r = threadIdx.x; r < (1 << (T - U)); r += blockDim.x) {
+      sh.rl[r] = swz(deposit32(r, full & ~sh.wml_c));
+      sh.plp[r] = swz(deposit32(r, full & ~sh.wml_p));
+    }
+    if (g > 0) {
+      // stage P = (new gate)^H and Q = (replaced gate)^H of each previous
+      // step, one thread per (step, entry)
+      const int ns = prv.cnt < GMAXSTEPS ? prv.cnt : GMAXSTEPS;
+      for (int t = threadIdx.x; t < ns * 16; t += blockDim.x) {
+        const int st = t / 16, e = t % 16;
+        int64_t slot;
+        int q, k;
+        if (!bwd_step(bd, arity, L, n, b, prv.j0 + st, &slot, &q, &k)) continue;
+        const int m = 1 << k;
+        if (e >= m * m) continue;
+        const int r = e / m, c = e % m;
+        const double2 vn = cconj(gates[bd.gate_off[b] + slot * 16 + c * m + r]);
+        const double2 vo = cconj(old_gates[((int64_t)b * GMAXSTEPS + st) * 16 + c * m + r]);
+        sh.gr[1][st][e] = cf((float)vn.x, (float)vn.x);
+        sh.gi[1][st][e] = cf((float)vn.y, (float)vn.y);
+        sh.gr[0][st][e] = cf((float)vo.x, (float)vo.x);
+        sh.gi[0][st][e] = cf((float)vo.y, (float)vo.y);
+      }
+    }
+    __syncthreads();
+    if (U == 4) pass_chunk<4>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
+    else if (U == 3) pass_chunk<3>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
+    else pass_chunk<2>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
+  }
+}
+
+// ---- per-group polar kernel ------------------------------------------------------
+
+// M <- G^T M on the rows of gate bits (h, l): the target-side update z <- P z
+// with P = G^H maps M to conj(P) M = G^T M.
+__device__ void m_rows(double2* M, int D, const double2* G, int k, int h, int l) {
+  if (k == 2) {
+    const int items = D * (D / 4);
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int col = it % D, o = it / D;
+      int ob = 0, kk = 0;
+      for (int bit = 0; (1 << bit) < D; ++bit) {
+        if (bit == h || bit == l) continue;
+        ob |= ((o >> kk) & 1) << bit;
+        ++kk;
+      }
+      const int idx[4] = {ob, ob | (1 << l), ob | (1 << h), ob | (1 << h) | (1 << l)};
+      double2 x[4], y[4];
+      for (int r = 0; r < 4; ++r) x[r] = M[idx[r] * GM + col];
+      for (int r = 0; r < 4; ++r) {
+        double2 s = czero();
+        for (int rp = 0; rp < 4; ++rp) s = cadd(s, cmul(G[rp * 4 + r], x[rp]));
+        y[r] = s;
+      }
+      for (int r = 0; r < 4; ++r) M[idx[r] * GM + col] = y[r];
+    }
+  } else {
+    const int items = D * (D / 2);
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int col = it % D, o = it / D;
+      const int ob = ((o >> h) << (h + 1)) | (o & ((1 << h) - 1));
+      const double2 x0 = M[ob * GM + col], x1 = M[(ob | (1 << h)) * GM + col];
+      M[ob * GM + col] = cadd(cmul(G[0], x0), cmul(G[2], x1));
+      M[(ob | (1 << h)) * GM + col] = cadd(cmul(G[1], x0), cmul(G[3], x1));
+    }
+  }
+}
+
+// M <- M Q^T on the columns of gate bits (h, l), Q = G^H: the circuit-side
+// peel x <- Q x.  (M Q^T)[i][c] = sum_c' M[i][c'] conj(G[c'][c]).
+__device__ void m_cols(double2* M, int D, const double2* G, int k, int h, int l) {
+  if (k == 2) {
+    const int items = D * (D / 4);
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int row = it % D, o = it / D;
+      int ob = 0, kk = 0;
+      for (int bit = 0; (1 << bit) < D; ++bit) {
+        if (bit == h || bit == l) continue;
+        ob |= ((o >> kk) & 1) << bit;
+        ++kk;
+      }
+      const int idx[4] = {ob, ob | (1 << l), ob | (1 << h), ob | (1 << h) | (1 << l)};
+      double2 x[4], y[4];
+      for (int c = 0; c < 4; ++c) x[c] = M[row * GM + idx[c]];
+      for (int c = 0; c < 4; ++c) {
+        double2 s = czero();
+        for (int cp = 0; cp < 4; ++cp) s = cadd(s, cmul(cconj(G[cp * 4 + c]), x[cp]));
+        y[c] = s;
+      }
+      for (int c = 0; c < 4; ++c) M[row * GM + idx[c]] = y[c];
+    }
+  } else {
+    const int items = D * (D / 2);
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int row = it % D, o = it / D;
+      const int ob = ((o >> h) << (h + 1)) | (o & ((1 << h) - 1));
+      const double2 x0 = M[row * GM + ob], x1 = M[row * GM + (ob | (1 << h))];
+      M[row * GM + ob] = cadd(cmul(cconj(G[0]), x0), cmul(cconj(G[2]), x1));
+      M[row * GM + (ob | (1 << h))] = cadd(cmul(cconj(G[1]), x0), cmul(cconj(G[3]), x1));
+    }
+  }
+}
+
+// One block per state and group.  The polar factor of each step is the
+// sweep polar of small_linalg.h: singular values of E at most 1e-6 of the
+// largest count as zero, and on that null space (inputs the circuit never
+// feeds the gate, such as fresh |0> qubits) every completion is optimal, so
+// the kernel keeps the one nearest to the current gate; structured gates
+// stay structured under fp32 rounding.  nuc[b] receives Re Tr(W^H E) of the
+// last step, |<t|new|psi>| after the update.
+#define POLAR_THREADS 64
+
+__global__ void __launch_bounds__(POLAR_THREADS) k_group_polar(BatchDev bd, GroupDev gd, int g, double2* gates,
+                                                               const signed char* arity, const int* nlayers,
+                                                               const int* active, double* nuc) {
+  __shared__ double2 M[GMM];
+  __shared__ double2 env[16];
+  for (int b = blockIdx.x; b < bd.B; b += gridDim.x) {
+    if (active && !active[b]) continue;
+    if (g >= gd.ngroups[b]) continue;
+    const GroupEnt ge = gd.grp[(int64_t)b * gd.gmax + g];
+    const int n = bd.n[b], L = nlayers[b], D = 1 << ge.u;
+    const int c0 = gd.state_chunk0[b], nc = gd.state_nchunks[b];
+    __syncthreads();
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+      const int i = e / D, k = e % D;
+      double2 s = czero();
+      for (int c = 0; c < nc; ++c) s = cadd(s, gd.partials[(int64_t)(c0 + c) * GMM + i * GM + k]);
+      M[i * GM + k] = s;
+    }
+    __syncthreads();
+    const double2* pend = nullptr;
+    int pk = 0, ph = 0, pl = 0;
+    for (int s = 0; s < ge.cnt && s < GMAXSTEPS; ++s) {
+      int64_t slot;
+      int q, k;
+      if (!bwd_step(bd, arity, L, n, b, ge.j0 + s, &slot, &q, &k)) continue;
+      double2* gptr = gates + bd.gate_off[b] + slot * 16;
+      const int h = __popc(ge.qmask >> (q + 1)), l = k == 2 ? __popc(ge.qmask >> (q + 2)) : 0;
+      if (pend) {
+        m_rows(M, D, pend, pk, ph, pl);
+        __syncthreads();
+      }
+      m_cols(M, D, gptr, k, h, l);
+      __syncthreads();
+      const int m = 1 << k;
+      if (threadIdx.x < m * m) {
+        const int r = threadIdx.x / m, c = threadIdx.x % m;
+        double2 acc = czero();
+        for (int o = 0; o < D / m; ++o) {
+          int ob = 0, kk = 0;
+          for (int bit = 0; (1 << bit) < D; ++bit) {
+            if (bit == h || (k == 2 && bit == l)) continue;
+            ob |= ((o >> kk) & 1) << bit;
+            ++kk;
+          }
+          const int ir = ob | (k == 2 ? (((r >> 1) & 1) << h) | ((r & 1) << l) : (r << h));
+          const int ic = ob | (k == 2 ? (((c >> 1) & 1) << h) | ((c & 1) << l) : (c << h));
+          acc = cadd(acc, M[ir * GM + ic]);
+        }
+        env[threadIdx.x] = acc;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double2 e[16], w[16], wprev[16];
+        bool finite = true;
+        for (int i = 0; i < m * m; ++i) {
+          e[i] = env[i];
+          finite = finite && isfinite(e[i].x) && isfinite(e[i].y);
+        }
+        double2* keep = gd.old_gates + ((int64_t)b * GMAXSTEPS + s) * 16;
+        for (int i = 0; i < m * m; ++i) keep[i] = gptr[i];
+        if (!finite) {
+          atomicOr(bd.err, KERR_NONFINITE);
+        } else {
+          for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
+          const double nn = polar_sweep(e, m, w, wprev);
+          for (int i = 0; i < m * m; ++i) gptr[i] = cconj(w[i]);
+          nuc[b] = nn;
+        }
+      }
+      __syncthreads();
+      pend = gptr;
+      pk = k;
+      ph = h;
+      pl = l;
+    }
+  }
+}
+
+// ---- launches ----------------------------------------------------------------------
+
+void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, const int* nlayers,
+                       cudaStream_t s) {
+  qm_note_launch();
+  const int blocks = (bd.B + 127) / 128;
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers);
+}
+
+int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
+                      const double2* gates, const signed char* arity, const int* nlayers, const int* active,
+                      cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_group_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)PASS_DYN_SMEM);
+    if (e != cudaSuccess) return (int)e;
+    attr_set = true;
+  }
+  int grid = gd.nchunks < 152 ? gd.nchunks : 152;   // one block per SM
+  if (grid < 1) grid = 1;
+  qm_note_launch();
+  k_group_pass<<<grid, BLOCK_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,
+                                                          nlayers, active);
+  return 0;
+}
+
+void launch_group_polar(const BatchDev& bd, const GroupDev& gd, int g, double2* gates, const signed char* arity,
+                        const int* nlayers, const int* active, double* nuc, cudaStream_t s) {
+  qm_note_launch();
+  k_group_polar<<<bd.B, POLAR_THREADS, 0, s>>>(bd, gd, g, gates, arity, nlayers, active, nuc);
+}

@@ -49,15 +49,15 @@ int64_t qmprs_launch_count(void);
 
 /*
  * Per-kernel profiling of qmprs_optimize_layers (instrumentation, no
- * reference counterpart).  When enabled, every launch of the three sweep
- * kernel classes is bracketed by CUDA events on the caller's stream;
- * qmprs_plan_profile returns, for kernel 0 (environment stream: peel the
- * gate off the circuit state and accumulate the environment), 1 (target
- * update), 2 (circuit rebuild) or 3 (environment reduce + polar update), the
- * launches, the summed event time in ms and the algorithmic bytes moved
- * (complex64 reads and writes of the states active in each launch; 0 for
- * kernel 3).  Enabling resets the counters; profiling synchronises once per
- * sweep.
+ * reference counterpart).  When enabled, every launch of the sweep kernel
+ * classes is bracketed by CUDA events on the caller's stream;
+ * qmprs_plan_profile returns, for kernel 0 (group pass: apply the previous
+ * group's gates and reduce the cross matrix of the next), 2 (circuit
+ * rebuild) or 3 (per-group step algebra and polar updates; class 1 is
+ * unused), the launches, the summed event time in ms and the algorithmic
+ * bytes moved (complex64 reads and writes of the states active in each
+ * launch; 0 for kernel 3).  Enabling resets the counters; profiling
+ * synchronises once per sweep.
  */
 int qmprs_plan_set_profiling(qmprs_plan_t p, int enable);
 int qmprs_plan_profile(qmprs_plan_t p, int kernel, int64_t* launches, double* milliseconds, double* bytes);
@@ -191,6 +191,65 @@ int qmprs_overlap_noalloc(const void* a, const void* b, int num_states, const in
  */
 int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t* arity, int layer,
                       int inverse, void* stream);
+
+/*
+ * Learned warm start (no reference counterpart: the reference initialises
+ * the layers analytically only).  Building blocks of the BF16 multilayer
+ * perceptron that predicts a block's converged gate from its analytic
+ * initial gate; qmprs_gb300.warmstart composes them into training and
+ * inference.  All matrices are row-major device buffers.
+ *
+ * qmprs_gemm_bf16: C = A B^T on the tensor cores (tcgen05.mma, BF16
+ * operands, FP32 accumulation in tensor memory).  A is M x K (leading
+ * dimension lda), B is N x K (ldb); M a multiple of 128, N a multiple of 16
+ * in [16, 256], K a multiple of 16, lda and ldb multiples of 8, A and B
+ * 16-byte aligned.  ksplit < K splits K over blocks (multiple of 16), which
+ * needs `part` (ceil(K / ksplit) * M * N floats) and reduces in fixed order.
+ * Epilogue: z = C + bias + resid (bias [N] and resid [M x ldr], fp32, may
+ * be NULL); Cf (fp32, ldc) receives z; Cb (bf16, ldc) and CbT (bf16,
+ * N x ldt, transposed) receive act(z), act 0 = identity, 1 = GELU (tanh
+ * form).  Any output may be NULL.  `err` is a device int; bit 16 is raised
+ * if a tensor-core completion wait ran out.
+ */
+int qmprs_gemm_bf16(const void* A, int lda, const void* B, int ldb, int M, int N, int K, int ksplit,
+                    const float* bias, const float* resid, int ldr, int act, float* Cf, int ldc, void* Cb,
+                    void* CbT, int ldt, float* part, int* err, void* stream);
+
+/*
+ * Gate loss of a batch of B predictions: Y and U are B x 32 floats (4 x 4
+ * complex, row-major, interleaved re/im), w the per-sample weights.
+ * loss[s] = w[s] min_phi |Y_s - e^{i phi} U_s|_F^2; dY = d(sum loss) / dY
+ * scaled by inv_wsum, also as bf16 (B x 32) and transposed bf16 (32 x ldt).
+ */
+int qmprs_mlp_loss(const float* Y, const float* U, const float* w, int B, float inv_wsum, float* loss, float* dY,
+                   void* dYb, void* dYT, int ldt, void* stream);
+
+/* dZ = dH * GELU'(Z) for B x N; also bf16 and transposed bf16 (N x ldt). */
+int qmprs_mlp_act_back(const float* dH, const float* Z, int B, int N, float* dZ, void* dZb, void* dZT, int ldt,
+                       void* stream);
+
+/* out[c] = sum over the B rows of X[r][c] (B x N), fixed order. */
+int qmprs_mlp_col_sum(const float* X, int B, int N, float* out, void* stream);
+
+/*
+ * One Adam step (bias-corrected, step >= 1, decoupled weight decay wd) on
+ * fp32 master weights W (rows x cols) with gradient G (the same layout, or
+ * cols x rows when gT != 0); refreshes the bf16 copies Wb (rows x cols) and
+ * WTb (cols x rows) when given.
+ */
+int qmprs_mlp_adam(float* W, const float* G, int gT, float* m, float* v, int rows, int cols, float lr, float b1,
+                   float b2, float eps, int step, float wd, void* Wb, void* WTb, void* stream);
+
+/*
+ * Project network outputs to gates: row r of Y (4 x 4 complex, interleaved
+ * fp32; for kind[r] == 1 the 2 x 2 in its first four entries) becomes its
+ * unitary polar factor, written to the complex128 gate slot slots[r] (units
+ * of 16 entries) of `gates`; singular directions below 1e-6 of the largest
+ * are completed towards the gate already in the slot.  Rows with non-finite
+ * entries leave the slot unchanged.
+ */
+int qmprs_mlp_project(const float* Y, int rows, const int64_t* slots, const int8_t* kind, void* gates,
+                      void* stream);
 
 #ifdef __cplusplus
 }

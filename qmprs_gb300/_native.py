@@ -53,6 +53,19 @@ SIGNATURES: dict[str, tuple] = {
     "qmprs_apply_layer": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int, ctypes.c_int,
                                          _c_void_p]),
     "qmprs_overlap_noalloc": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, _c_int_p, _c_void_p, _c_void_p]),
+    "qmprs_gemm_bf16": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, _c_void_p, _c_void_p, ctypes.c_int, ctypes.c_int,
+                                       _c_void_p, ctypes.c_int, _c_void_p, _c_void_p, ctypes.c_int, _c_void_p,
+                                       _c_void_p, _c_void_p]),
+    "qmprs_mlp_loss": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, ctypes.c_int, ctypes.c_float, _c_void_p,
+                                      _c_void_p, _c_void_p, _c_void_p, ctypes.c_int, _c_void_p]),
+    "qmprs_mlp_act_back": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, ctypes.c_int, _c_void_p, _c_void_p,
+                                          _c_void_p, ctypes.c_int, _c_void_p]),
+    "qmprs_mlp_col_sum": (ctypes.c_int, [_c_void_p, ctypes.c_int, ctypes.c_int, _c_void_p, _c_void_p]),
+    "qmprs_mlp_adam": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, _c_void_p, _c_void_p, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_int, ctypes.c_float, _c_void_p, _c_void_p, _c_void_p]),
+    "qmprs_mlp_project": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
 }
 
 _lib = None

@@ -53,6 +53,7 @@ enum {
   KERR_EIG_WIDTH = 2,
   KERR_NONFINITE = 4,
   KERR_BAD_GATE = 8,
+  KERR_TC_TIMEOUT = 16,   // a tensor-core completion wait ran out
 };
 
 struct BatchDev {

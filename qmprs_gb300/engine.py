@@ -301,6 +301,27 @@ class Engine:
         counts = torch.tensor([2 ** (n + 1) for n in ns], dtype=torch.int64, device="cuda")
         return vec * torch.repeat_interleave(inv, counts)
 
+    def _fallback(self, p: Plan, target, sv, analytic, gates, arity, nl, sf, sd, ov, nn, num_sweeps: int,
+                  stop_fidelity: float):
+        """States of a warm-started batch that end below stop_fidelity are
+        swept from their analytic layers; each state keeps the better run."""
+        fid = torch.sqrt(ov[0::2] ** 2 + ov[1::2] ** 2) / torch.sqrt(nn[0::2])
+        if not bool((fid < stop_fidelity).any().item()):
+            return gates, sf, sd, ov
+        sf2, sd2 = self.stage_sweeps(p, target, analytic, arity, nl, num_sweeps, stop_fidelity)
+        ov2 = self.overlap(p, self.stage_circuit(p, analytic, arity, nl), sv)
+        fid2 = torch.sqrt(ov2[0::2] ** 2 + ov2[1::2] ** 2) / torch.sqrt(nn[0::2])
+        take = (fid < stop_fidelity) & (fid2 > fid)                       # per state
+        per_slot = torch.repeat_interleave(take, torch.as_tensor(
+            [p.max_layers * n * 32 for n in p.nqubits], device=take.device))
+        gates = torch.where(per_slot, analytic, gates)
+        S = max(int(num_sweeps), 0)
+        if S > 0:
+            sf = torch.where(torch.repeat_interleave(take, S)[: sf.numel()], sf2, sf)
+        sd = torch.where(take, sd2, sd)
+        ov = torch.where(torch.repeat_interleave(take, 2), ov2, ov)
+        return gates, sf, sd, ov
+
     @staticmethod
     def _sp(stream) -> ctypes.c_void_p:
         st = stream or torch.cuda.current_stream()
@@ -309,7 +330,7 @@ class Engine:
     # ---- whole path ------------------------------------------------------------
     def encode(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
                fidelity_threshold: float = 1 - 1e-6, stop_fidelity: float = 0.0,
-               keep_tensors: bool = False, nqubits=None, download: bool = True) -> BatchResult:
+               keep_tensors: bool = False, nqubits=None, download: bool = True, warm_start=None) -> BatchResult:
         """``prepare_state`` for a batch: (a) -> (b)+(c) -> (d) -> fidelity.
 
         ``statevectors`` is either a list of complex arrays, or (with
@@ -317,6 +338,12 @@ class Engine:
         amplitudes of all states back to back, resident on the GPU or in
         (pinned) host memory.  Inputs need not be normalised: the reported
         fidelity is ``|<sv|C|0>| / ||sv||``.
+
+        ``warm_start`` (a ``warmstart.WarmStartMLP``) replaces the analytic
+        layers by the network's predictions before the sweeps; with
+        ``stop_fidelity > 0`` every state that ends below it is swept again
+        from its analytic layers (the plain method) and keeps the better of
+        the two results.
         """
         if nqubits is None:
             p, sv = self.upload(statevectors, num_layers, bond_dimension)
@@ -329,10 +356,18 @@ class Engine:
                 sv = sv.to("cuda", non_blocking=True)
         tensors, bonds, target = self.stage_mps(p, sv, bond_dimension)
         gates, arity, nl, lf = self.stage_layers(p, target, num_layers, fidelity_threshold)
+        analytic = None
+        if warm_start is not None:
+            from . import warmstart as _ws
+            analytic = gates.clone()
+            _ws.predict_layers(warm_start, gates, p.gate_off, p.nqubits, nl.cpu().numpy())
         sf, sd = self.stage_sweeps(p, target, gates, arity, nl, num_sweeps, stop_fidelity)
         circ = self.stage_circuit(p, gates, arity, nl)
         ov = self.overlap(p, circ, sv)
         nn = self.overlap(p, sv, sv)
+        if analytic is not None and stop_fidelity > 0.0:
+            gates, sf, sd, ov = self._fallback(p, target, sv, analytic, gates, arity, nl, sf, sd, ov, nn,
+                                               num_sweeps, stop_fidelity)
         B, S = p.B, max(int(num_sweeps), 0)
         if not download:
             return BatchResult(nqubits=p.nqubits, gates=gates, arity=arity, num_layers=nl, layer_fidelities=lf,

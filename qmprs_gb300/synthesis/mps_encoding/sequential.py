@@ -148,7 +148,7 @@ class Sequential(MPSEncoder):
 
     # ---- batched extension -------------------------------------------------------------
     def prepare_states(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
-                       stop_fidelity: float = 0.0, emit: bool = True, nqubits=None):
+                       stop_fidelity: float = 0.0, emit: bool = True, nqubits=None, *, warm_start=None):
         """Encode many statevectors at once (any mix of qubit counts).
 
         Same result per state as ``prepare_state`` (default
@@ -159,6 +159,9 @@ class Sequential(MPSEncoder):
         complex64 amplitudes of all states back to back; packed inputs are
         normalised on the device.  Returns the list of circuits
         (``emit=True``, else None) and the engine's BatchResult.
+        ``warm_start`` (keyword only; a ``qmprs_gb300.warmstart.WarmStartMLP``)
+        starts the sweeps from the network's predicted layers; states that
+        end below ``stop_fidelity`` fall back to the analytic layers.
         """
         if not isinstance(num_layers, int) or num_layers < 1:
             raise ValueError("The number of layers must be a positive integer.")
@@ -170,14 +173,14 @@ class Sequential(MPSEncoder):
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
             res = eng.encode(statevectors, bond_dimension, num_layers, num_sweeps, self.fidelity_threshold,
-                             stop_fidelity, nqubits=ns)
+                             stop_fidelity, nqubits=ns, warm_start=warm_start)
         else:
             kets = [sv if isinstance(sv, Ket) else Ket(sv) for sv in statevectors]
             ns = [k.num_qubits for k in kets]
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
             res = eng.encode([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
-                             self.fidelity_threshold, stop_fidelity)
+                             self.fidelity_threshold, stop_fidelity, warm_start=warm_start)
         circuits = None
         if emit:
             circuits = []

@@ -1,0 +1,208 @@
+"""Warm-start network on the GPU: the tcgen05 GEMM against torch, forward and
+backward against the numpy oracle (oracle/mlp.py), training, and the layer
+prediction path."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp as OM
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ws():
+    from qmprs_gb300 import warmstart
+    return warmstart
+
+
+def _bf(x):
+    return torch.as_tensor(x, device="cuda").to(torch.bfloat16).contiguous()
+
+
+@pytest.mark.parametrize("M,N,K,ksplit", [(128, 16, 16, 0), (128, 32, 64, 0), (256, 256, 128, 0),
+                                          (128, 128, 256, 0), (256, 32, 1024, 256), (384, 64, 48, 0),
+                                          (128, 256, 2048, 512)])
+def test_gemm_tc_matches_torch(ws, M, N, K, ksplit):
+    rng = np.random.default_rng(M + N + K)
+    a = _bf(rng.standard_normal((M, K)).astype(np.float32))
+    b = _bf(rng.standard_normal((N, K)).astype(np.float32))
+    c = torch.full((M, N), float("nan"), device="cuda")
+    S = max(1, -(-K // ksplit)) if ksplit else 1
+    part = torch.zeros(S * M * N, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    code = ws.N.load().qmprs_gemm_bf16(ws._p(a), K, ws._p(b), K, M, N, K, ksplit, None, None, 0, 0, ws._p(c), N,
+                                       None, None, 0, ws._p(part), ws._p(err), ws._sp(None))
+    assert code == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = a.float() @ b.float().t()
+    rel = (c - ref).norm() / ref.norm()
+    assert rel < 1e-5, float(rel)
+
+
+def test_gemm_epilogue_bias_gelu_transpose(ws):
+    rng = np.random.default_rng(3)
+    M, N, K = 256, 64, 128
+    a = _bf(rng.standard_normal((M, K)).astype(np.float32) * 0.3)
+    b = _bf(rng.standard_normal((N, K)).astype(np.float32) * 0.3)
+    bias = torch.as_tensor(rng.standard_normal(N).astype(np.float32), device="cuda")
+    res = torch.as_tensor(rng.standard_normal((M, N + 8)).astype(np.float32), device="cuda")
+    z = torch.zeros(M, N, device="cuda")
+    h = torch.zeros(M, N, dtype=torch.bfloat16, device="cuda")
+    ht = torch.zeros(N, M, dtype=torch.bfloat16, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    code = ws.N.load().qmprs_gemm_bf16(ws._p(a), K, ws._p(b), K, M, N, K, 0, ws._p(bias), ws._p(res), N + 8, 1,
+                                       ws._p(z), N, ws._p(h), ws._p(ht), M, None, ws._p(err), ws._sp(None))
+    assert code == 0
+    torch.cuda.synchronize()
+    zr = a.float() @ b.float().t() + bias + res[:, :N]
+    assert torch.allclose(z, zr, rtol=1e-5, atol=1e-4)
+    g = OM.gelu(zr.double().cpu().numpy())
+    assert np.allclose(h.float().cpu().numpy(), g, rtol=1e-2, atol=1e-2)
+    assert torch.equal(ht, h.t())
+
+
+def test_gemm_rejects_bad_shapes(ws):
+    lib = ws.N.load()
+    a = torch.zeros(128, 64, dtype=torch.bfloat16, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    c = torch.zeros(128, 64, device="cuda")
+    # M not a multiple of 128, N not a multiple of 16, N > 256, K not a multiple of 16
+    for M, N, K in [(100, 64, 64), (128, 24, 64), (128, 512, 64), (128, 64, 40)]:
+        assert lib.qmprs_gemm_bf16(ws._p(a), 64, ws._p(a), 64, M, N, K, 0, None, None, 0, 0, ws._p(c), 64, None,
+                                   None, 0, None, ws._p(err), ws._sp(None)) == 1
+
+
+def test_mlp_forward_backward_match_oracle(ws):
+    rng = np.random.default_rng(11)
+    model = ws.WarmStartMLP(seed=5)
+    model.load_params(OM.init_params(ws.DIMS, 9))   # non-zero output layer
+    rows = 200
+    x = np.zeros((rows, ws.DIMS[0]), np.float32)
+    x[:, :ws.FEAT] = rng.standard_normal((rows, ws.FEAT)).astype(np.float32) * 0.5
+    u = rng.standard_normal((rows, 32)).astype(np.float32) * 0.3
+    w = np.ones(rows, np.float32)
+    w[::7] = 0.5
+    xt = torch.as_tensor(x, device="cuda")
+    y = model.forward(xt, train=True).cpu().numpy()
+    loss, grads = model.backward(torch.as_tensor(u, device="cuda"), torch.as_tensor(w, device="cuda"))
+    torch.cuda.synchronize()
+    params = model.params()
+    yo, cache = OM.forward(params, OM.bf16(x), residual=x[:, :32])
+    assert np.linalg.norm(y - yo) / np.linalg.norm(yo) < 2e-3
+    lo, dyo = OM.loss_and_grad(yo, u.astype(np.float64), w.astype(np.float64))
+    assert abs(loss - lo.sum() / w.sum()) < 1e-3 * max(1.0, abs(loss))
+    go = OM.backward(params, cache, dyo)
+    for j, ((dW, db, tr), (dWo, dbo)) in enumerate(zip(grads, go)):
+        g = dW.cpu().numpy()
+        if tr:
+            g = g.T
+        assert np.linalg.norm(g - dWo) / np.linalg.norm(dWo) < 2e-2, j
+        assert np.linalg.norm(db.cpu().numpy() - dbo) / max(np.linalg.norm(dbo), 1e-12) < 2e-2, j
+
+
+def test_mlp_training_learns_a_gate_map(ws):
+    """The network learns a smooth gate map, U -> V U for a fixed unitary V,
+    on top of its residual (the input gate): the loss drops by more than
+    10x."""
+    rng = np.random.default_rng(2)
+    rows = 8192
+    q = np.linalg.qr(rng.standard_normal((rows, 4, 4)) + 1j * rng.standard_normal((rows, 4, 4)))[0]
+    v = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))[0]
+    v = 0.7 * np.eye(4) + 0.3 * v
+    v = np.linalg.svd(v)[0] @ np.linalg.svd(v)[2]
+    t = v[None] @ q
+    g = np.stack([q.real, q.imag], -1).reshape(rows, 32).astype(np.float32)
+    tg = np.stack([t.real, t.imag], -1).reshape(rows, 32).astype(np.float32)
+    x = np.zeros((rows, ws.DIMS[0]), np.float32)
+    x[:, :32] = g
+    model = ws.WarmStartMLP(seed=1)
+    xt, yt = torch.as_tensor(x, device="cuda"), torch.as_tensor(tg, device="cuda")
+    hist = model.train(xt, yt, epochs=20, batch=1024, lr=2e-3)
+    assert hist[-1] < hist[0] / 10, hist
+
+
+def test_predict_layers_gives_unitary_gates(ws):
+    from qmprs_gb300 import engine as E
+    eng = E.engine()
+    ns = [8, 9, 10, 8]
+    sv = eng.random_mps_states(ns, [4, 4, 8, 2], seed=3)
+    p = eng.plan(ns, 3, 16)
+    _, _, target = eng.stage_mps(p, sv, 16)
+    gates, arity, nl, _ = eng.stage_layers(p, target, 3, 1 - 1e-6)
+    nlh = nl.cpu().numpy()
+    before = gates.clone()
+    model = ws.WarmStartMLP(seed=0)
+    cnt = ws.predict_layers(model, gates, p.gate_off, ns, nlh)
+    torch.cuda.synchronize()
+    assert cnt == sum(int(L) * n for n, L in zip(ns, nlh))
+    blocks = ws.block_index(ns, nlh)
+    slots = ws.slots_of(p.gate_off, ns, blocks)
+    kind = ws.block_kind(ns, blocks)
+    ar = arity.cpu().numpy()
+    assert np.array_equal(ar[slots], kind)
+    g = gates.cpu().numpy().view(np.complex128).reshape(-1, 16)
+    b0 = before.cpu().numpy().view(np.complex128).reshape(-1, 16)
+    for sl, k in zip(slots, kind):
+        m = 2 ** int(k)
+        u = g[sl][: m * m].reshape(m, m)
+        assert np.allclose(u.conj().T @ u, np.eye(m), atol=1e-9)
+        assert np.array_equal(g[sl][m * m:], b0[sl][m * m:])
+    # an untrained network's output is the analytic gate itself
+    diff = max(np.abs(g[sl] - b0[sl]).max() for sl in slots)
+    assert diff < 1e-5
+    sf, sd = eng.stage_sweeps(p, target, gates, arity, nl, 2, 0.0)
+    torch.cuda.synchronize()
+    assert np.all(np.isfinite(sf.cpu().numpy()))
+
+
+def _pairs(ws, eng, ns, bonds, layers, sweeps, seed):
+    from qmprs_gb300 import warmstart_train as T
+    return T.make_pairs(eng, ns, bonds, layers, sweeps, 32, seed=seed, log=lambda *_: None)
+
+
+def test_trained_network_gains_on_held_out_gates(ws):
+    """What the network gains over the method without it, per gate: on
+    held-out states its predictions are closer (phase-invariant Frobenius
+    loss) to the gates the sweeps converge to than the analytic gates are.
+    The effect on the sweeps' fidelity is measured by
+    qmprs_gb300.warmstart_train and reported in the design notes; it is not
+    asserted here."""
+    from qmprs_gb300 import engine as E
+    eng = E.engine()
+    rng = np.random.default_rng(4)
+    ns = [int(x) for x in rng.integers(10, 13, size=384)]
+    bonds = [int(x) for x in rng.choice([4, 8, 16], size=384)]
+    x, y = _pairs(ws, eng, ns[:320], bonds[:320], 4, 5, seed=100)
+    xh, yh = _pairs(ws, eng, ns[320:], bonds[320:], 4, 5, seed=200)
+    model = ws.WarmStartMLP(seed=3)
+    base = ws.WarmStartMLP(seed=3)          # untrained: the analytic gates
+    model.train(x, y, epochs=40, batch=2048, lr=1e-3)
+
+    def held_out_loss(m):
+        out = m.forward(xh).cpu().numpy().astype(np.float64)
+        loss, _ = OM.loss_and_grad(out, yh.cpu().numpy().astype(np.float64), np.ones(len(out)))
+        return float(loss.mean())
+
+    lm, lb = held_out_loss(model), held_out_loss(base)
+    print(f"held-out gate loss: trained {lm:.4f}, analytic {lb:.4f}")
+    assert lm < 0.97 * lb, (lm, lb)
+
+
+def test_warm_start_api_and_fallback(ws):
+    """encode(warm_start=...) with an untrained network equals the plain
+    path; with a network that ruins the layers, states below stop_fidelity
+    fall back to the analytic layers and are never worse than plain."""
+    from qmprs_gb300 import engine as E
+    eng = E.engine()
+    ns = [8, 9, 10, 9, 8, 10]
+    sv = eng.random_mps_states(ns, [2, 4, 4, 8, 2, 4], seed=12)
+    plain = eng.encode(sv.clone(), 16, 3, 3, nqubits=ns)
+    same = eng.encode(sv.clone(), 16, 3, 3, nqubits=ns, warm_start=ws.WarmStartMLP(seed=0))
+    assert np.allclose(plain.fidelity, same.fidelity, atol=1e-5)
+    bad = ws.WarmStartMLP(seed=0)
+    bad.load_params(OM.init_params(ws.DIMS, 1))
+    res = eng.encode(sv.clone(), 16, 3, 3, nqubits=ns, stop_fidelity=0.999999, warm_start=bad)
+    assert np.all(res.fidelity >= plain.fidelity - 1e-5)

@@ -31,10 +31,62 @@ __host__ __device__ inline int chi_eff(int chi, int n) {
 
 __device__ __forceinline__ bool bond_ok(int r) { return r >= 1 && r <= TT_MAXB; }
 
+// Compensated accumulation of exact products (double-float): p = u v is
+// split exactly into ph + pl (fma), ph enters (hi, lo) through a TwoSum and
+// pl and the TwoSum error land in lo.  Flushed to fp64 every TT_FLUSH rows,
+// the relative error of a Gram entry is about TT_FLUSH * 2^-48 of the sum of
+// |products|, far below the 1e-10 truncation cutoff the eigenvalues decide.
+struct DF {
+  float hi, lo;
+};
+
+// Every operation is an explicitly rounded intrinsic, so the compiler never
+// contracts the product into the sum (which would break the error terms).
+__device__ __forceinline__ void df_add_prod(DF& s, float u, float v) {
+  const float ph = __fmul_rn(u, v);
+  const float pl = __fmaf_rn(u, v, -ph);
+  const float t = __fadd_rn(s.hi, ph);
+  const float bv = __fsub_rn(t, s.hi);
+  const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, bv)), __fsub_rn(ph, bv));
+  s.lo = __fadd_rn(s.lo, __fadd_rn(err, pl));
+  s.hi = t;
+}
+
+#define TT_FLUSH 32
+#define TT_EPB 8   // entries per thread: a 2 x 4 block (a in {2i, 2i+1}, cc in {4j .. 4j+3})
+
+// Entry block e of the upper triangle of a w x w Gram, ordered by column
+// block j (2j + 2 blocks in column block j, capped at w / 2 rows).
+__device__ __forceinline__ void gram_block(int e, int w, int* i0, int* j0) {
+  const int half = w >> 1;
+  int j = 0, base = 0;
+  for (;; ++j) {
+    const int cnt = min(half, 2 * j + 2);
+    if (e < base + cnt) break;
+    base += cnt;
+  }
+  *i0 = e - base;
+  *j0 = j;
+}
+
+__device__ __forceinline__ int gram_nblocks(int w) {
+  const int half = w >> 1, nj = (w + 3) / 4;
+  int t = 0;
+  for (int j = 0; j < nj; ++j) t += min(half, 2 * j + 2);
+  return t;
+}
+
+// Upper triangle of M^H M (M = the 2^c x w remainder) per state: up to
+// TT_SPLIT blocks per state take row ranges; in a block, thread t takes the
+// entry block (t mod nb) and every (256 / nb)-th row of the range, sums
+// exact fp32 products with compensation and flushes to fp64; the rest
+// groups are then summed in fixed order through shared memory.  The last
+// block of a state (ticket) sums the splits in order and mirrors the lower
+// triangle.
 __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step, const float2* sv,
                                                            const float2* src, const int* bonds,
                                                            double2* partials, double2* gram) {
-  __shared__ float2 xs[TT_CH][TT_MAXW];
+  __shared__ double2 red[BLOCK_THREADS * TT_EPB];   // 32 KB
   const int WW = TT_MAXW * TT_MAXW;
   for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
     const int b = bd.tile_state[tile];
@@ -56,42 +108,74 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
     int64_t lo, hi;
     tile_range(ipow2(c), idx, nsplit, &lo, &hi);
     double2* part = partials + ((int64_t)b * TT_SPLIT + idx) * WW;
-    for (int e0 = 0; e0 < w * w; e0 += 16 * BLOCK_THREADS) {
-      double2 acc[16];
+    const int nb = gram_nblocks(w);
+    for (int e0 = 0; e0 < nb; e0 += BLOCK_THREADS) {
+      const int nbp = nb - e0 < BLOCK_THREADS ? nb - e0 : BLOCK_THREADS;
+      const int nsub = BLOCK_THREADS / nbp;
+      const int eb = threadIdx.x % nbp, sub = threadIdx.x / nbp;
+      const bool act = sub < nsub;
+      int bi = 0, bj = 0;
+      if (act) gram_block(e0 + eb, w, &bi, &bj);
+      const int a0 = 2 * bi, c0 = 4 * bj;
+      double2 acc[TT_EPB];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) acc[i] = czero();
-      for (int64_t r0 = lo; r0 < hi; r0 += TT_CH) {
-        const int nr = (int)((hi - r0) < TT_CH ? (hi - r0) : TT_CH);
-        __syncthreads();
-        for (int e = threadIdx.x; e < nr * w; e += blockDim.x) xs[e / w][e % w] = m[(r0 + e / w) * w + e % w];
-        __syncthreads();
+      for (int k = 0; k < TT_EPB; ++k) acc[k] = czero();
+      if (act) {
+        int64_t row = lo + sub;
+        while (row < hi) {
+          DF re[TT_EPB], im[TT_EPB];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int e = e0 + threadIdx.x + i * BLOCK_THREADS;
-          if (e < w * w) {
-            const int a = e / w, cc = e % w;
-            double2 s = acc[i];
-            for (int rr = 0; rr < nr; ++rr) {
-              const double2 x = f2d(xs[rr][a]), y = f2d(xs[rr][cc]);
-              s.x += x.x * y.x + x.y * y.y;
-              s.y += x.x * y.y - x.y * y.x;
-            }
-            acc[i] = s;
+          for (int k = 0; k < TT_EPB; ++k) re[k] = im[k] = DF{0.f, 0.f};
+          for (int f = 0; f < TT_FLUSH && row < hi; ++f, row += nsub) {
+            const float2* x = m + row * w;
+            float2 xa[2], xc[4];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) xa[u] = x[a0 + u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) xc[v] = c0 + v < w ? x[c0 + v] : cf(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+              for (int v = 0; v < 4; ++v) {
+                // conj(xa) * xc
+                df_add_prod(re[u * 4 + v], xa[u].x, xc[v].x);
+                df_add_prod(re[u * 4 + v], xa[u].y, xc[v].y);
+                df_add_prod(im[u * 4 + v], xa[u].x, xc[v].y);
+                df_add_prod(im[u * 4 + v], -xa[u].y, xc[v].x);
+              }
+          }
+#pragma unroll
+          for (int k = 0; k < TT_EPB; ++k) {
+            acc[k].x += (double)re[k].hi + (double)re[k].lo;
+            acc[k].y += (double)im[k].hi + (double)im[k].lo;
           }
         }
       }
+      // sum the row groups of each entry block in fixed order
+      __syncthreads();
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int e = e0 + threadIdx.x + i * BLOCK_THREADS;
-        if (e < w * w) part[e] = acc[i];
+      for (int k = 0; k < TT_EPB; ++k) red[threadIdx.x * TT_EPB + k] = acc[k];
+      __syncthreads();
+      for (int o = threadIdx.x; o < nbp * TT_EPB; o += BLOCK_THREADS) {
+        const int ebo = o / TT_EPB, k = o % TT_EPB;
+        double2 sacc = czero();
+        for (int sb = 0; sb < nsub; ++sb) sacc = cadd(sacc, red[(sb * nbp + ebo) * TT_EPB + k]);
+        int gi, gj;
+        gram_block(e0 + ebo, w, &gi, &gj);
+        const int a = 2 * gi + k / 4, cc = 4 * gj + k % 4;
+        if (a <= cc && cc < w) part[a * w + cc] = sacc;
       }
     }
     __syncthreads();
     if (last_tile_ticket(bd.ticket, b, nsplit)) {
       for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+        const int a = e / w, cc = e % w;
+        if (a > cc) continue;
         double2 s = czero();
-        for (int t = 0; t < nsplit; ++t) s = cadd(s, ld_cg(&partials[((int64_t)b * TT_SPLIT + t) * WW + e]));
-        gram[(int64_t)b * WW + e] = s;
+        for (int t = 0; t < nsplit; ++t) s = cadd(s, ld_cg(&partials[((int64_t)b * TT_SPLIT + t) * WW + a * w + cc]));
+        gram[(int64_t)b * WW + a * w + cc] = s;
+        if (a != cc) gram[(int64_t)b * WW + cc * w + a] = cconj(s);
+        else gram[(int64_t)b * WW + a * w + a] = cd(s.x, 0.0);
       }
       __syncthreads();
       if (threadIdx.x == 0) bd.ticket[b] = 0;

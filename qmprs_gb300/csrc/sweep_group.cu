@@ -63,17 +63,6 @@ __device__ __forceinline__ int64_t deposit_bits(int64_t v, int64_t mask) {
 // swz(a) ^ swz(b) and the offset tables below hold swizzled values.
 __device__ __forceinline__ int swz(int li) { return li ^ (((li >> 4) ^ (li >> 8)) & 15); }
 
-// (a.x * b.x + c.x, a.y * b.y + c.y) as one packed FP32 FMA.
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
-  float2 d;
-  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return d;
-}
-
 // ---- group plan --------------------------------------------------------------
 
 __global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers) {
@@ -125,14 +114,12 @@ struct PassShared {
   int rl[1 << (GT - GW)];   // rest index -> swizzled tile offset (current window)
   int plp[1 << (GT - GW)];  // rest index -> swizzled tile offset (previous window)
   int d0[64], d1[64];       // global offset of tile index li: d0[li & 63] | d1[li >> 6]
-  float2 gr[2][GMAXSTEPS][16];   // [peel | new][step]: (re, re) of the applied matrix
-  float2 gi[2][GMAXSTEPS][16];   // (im, im)
+  float2 gm[2][GMAXSTEPS][16];   // [peel | new][step]: the applied matrix, row-major complex
 };
 
-// Dynamic shared memory: two tile buffers (x and z, float2 each) and the
-// target side of the current tile duplicated as (re, re, im, im) for the
-// cross reduction.
-#define PASS_DYN_SMEM ((size_t)(4 * sizeof(float2) + sizeof(float4)) * (1 << GT))
+// Dynamic shared memory: the tile of x and of z (float2 each).  Two blocks
+// share an SM, so one block's loads overlap the other's arithmetic.
+#define PASS_DYN_SMEM ((size_t)(2 * sizeof(float2)) * (1 << GT))
 
 // tile-local bit of global position p (p must be in pos_mask)
 __device__ __forceinline__ int tile_bit(int pos_mask, int p) { return __popc(pos_mask & ((1 << p) - 1)); }
@@ -148,115 +135,32 @@ __device__ __forceinline__ int deposit32(int v, int mask) {
   return r;
 }
 
-// y = G x on window bits (H, L), G given as gr[i] = (re, re), gi[i] = (im, im):
-// two packed accumulators pa = sum (gr xr, gr xi), pb = sum (gi xr, gi xi),
-// y = (pa.x - pb.y, pa.y + pb.x).  No operand needs a swap or a negation.
-template <int U, int H, int L>
-__device__ __forceinline__ void apply2_p(float2 (&a)[1 << U], const float2* gr, const float2* gi) {
-#pragma unroll
-  for (int o = 0; o < (1 << (U - 2)); ++o) {
-    const int b = win_other2<U, H, L>(o);
-    const int idx[4] = {b, b | (1 << L), b | (1 << H), b | (1 << H) | (1 << L)};
-    float2 x[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) x[c] = a[idx[c]];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      float2 pa = cf(0.f, 0.f), pb = cf(0.f, 0.f);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        pa = f2fma(gr[r * 4 + c], x[c], pa);
-        pb = f2fma(gi[r * 4 + c], x[c], pb);
-      }
-      a[idx[r]] = cf(pa.x - pb.y, pa.y + pb.x);
-    }
-  }
-}
-
-template <int U, int B>
-__device__ __forceinline__ void apply1_p(float2 (&a)[1 << U], const float2* gr, const float2* gi) {
-#pragma unroll
-  for (int o = 0; o < (1 << (U - 1)); ++o) {
-    const int b = win_other1<U, B>(o);
-    const float2 x0 = a[b], x1 = a[b | (1 << B)];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      float2 pa = f2fma(gr[r * 2 + 1], x1, f2fma(gr[r * 2], x0, cf(0.f, 0.f)));
-      float2 pb = f2fma(gi[r * 2 + 1], x1, f2fma(gi[r * 2], x0, cf(0.f, 0.f)));
-      a[r ? (b | (1 << B)) : b] = cf(pa.x - pb.y, pa.y + pb.x);
-    }
-  }
-}
-
-template <int U>
-__device__ __forceinline__ void apply_p(float2 (&a)[1 << U], const float2* gr, const float2* gi, int k, int hi,
-                                        int lo) {
-  if (k == 2) {
-    if (U == 2) {
-      apply2_p<U, 1, 0>(a, gr, gi);
-    } else if (U == 3) {
-      if (hi == 2 && lo == 1) apply2_p<U, 2, 1>(a, gr, gi);
-      else if (hi == 1 && lo == 0) apply2_p<U, 1, 0>(a, gr, gi);
-      else apply2_p<U, 2, 0>(a, gr, gi);
-    } else {
-      switch (hi * 4 + lo) {
-        case 3 * 4 + 2: apply2_p<U, 3, 2>(a, gr, gi); break;
-        case 3 * 4 + 1: apply2_p<U, 3, 1>(a, gr, gi); break;
-        case 3 * 4 + 0: apply2_p<U, 3, 0>(a, gr, gi); break;
-        case 2 * 4 + 1: apply2_p<U, 2, 1>(a, gr, gi); break;
-        case 2 * 4 + 0: apply2_p<U, 2, 0>(a, gr, gi); break;
-        default: apply2_p<U, 1, 0>(a, gr, gi); break;
-      }
-    }
-  } else {
-    switch (hi) {
-      case 0: apply1_p<U, 0>(a, gr, gi); break;
-      case 1: apply1_p<U, 1>(a, gr, gi); break;
-      case 2: if (U > 2) apply1_p<U, (U > 2 ? 2 : 0)>(a, gr, gi); break;
-      default: if (U > 3) apply1_p<U, (U > 3 ? 3 : 0)>(a, gr, gi); break;
-    }
-  }
-}
-
 // Previous group's peels on x and new gates on z, over the previous
-// window; z is also written duplicated into zd for the cross reduction.
-// With no previous group (g = 0) the tables describe the current window
-// and only the duplicate is written.
+// window: a thread owns the 2^U amplitudes of one window position and
+// applies the group's gates in registers.
 template <int U>
-__device__ __forceinline__ void pass_apply(const PassShared& sh, float2* xs, float2* zs, float4* zd, bool prev) {
+__device__ __forceinline__ void pass_apply(const PassShared& sh, float2* xs, float2* zs) {
   const int npos = 1 << (sh.T - U);
   for (int p = threadIdx.x; p < npos; p += blockDim.x) {
     const int po = sh.plp[p];
-    float2 a[1 << U];
-    if (prev) {
+    for (int side = 0; side < 2; ++side) {
+      float2* v = side ? zs : xs;
+      float2 a[1 << U];
 #pragma unroll
-      for (int w = 0; w < (1 << U); ++w) a[w] = xs[po ^ sh.wlp[w]];
+      for (int w = 0; w < (1 << U); ++w) a[w] = v[po ^ sh.wlp[w]];
       for (int s = 0; s < sh.npk; ++s)
-        if (sh.pk[s]) apply_p<U>(a, sh.gr[0][s], sh.gi[0][s], sh.pk[s], sh.phi[s], sh.plo[s]);
+        if (sh.pk[s]) win_apply<U>(a, sh.gm[side][s], sh.pk[s], sh.phi[s], sh.plo[s]);
 #pragma unroll
-      for (int w = 0; w < (1 << U); ++w) xs[po ^ sh.wlp[w]] = a[w];
-    }
-#pragma unroll
-    for (int w = 0; w < (1 << U); ++w) a[w] = zs[po ^ sh.wlp[w]];
-    if (prev) {
-      for (int s = 0; s < sh.npk; ++s)
-        if (sh.pk[s]) apply_p<U>(a, sh.gr[1][s], sh.gi[1][s], sh.pk[s], sh.phi[s], sh.plo[s]);
-    }
-#pragma unroll
-    for (int w = 0; w < (1 << U); ++w) {
-      const int li = po ^ sh.wlp[w];
-      if (prev) zs[li] = a[w];
-      zd[li] = make_float4(a[w].x, a[w].x, a[w].y, a[w].y);
+      for (int w = 0; w < (1 << U); ++w) v[po ^ sh.wlp[w]] = a[w];
     }
   }
 }
 
-// Cross reduction over this thread's rests for the 4 x 4 block (bi, bk):
-// aa[i * 4 + k] += (zr, zr) * x_k, bb[i * 4 + k] += (zi, zi) * x_k, so that
-// M = sum conj(z_i) x_k = (aa.x + bb.y, aa.y - bb.x).
+// acc[i * 4 + k] += conj(z[4 bi + i, r]) x[4 bk + k, r] over this thread's
+// rests (the 4 x 4 block (bi, bk) of M).
 template <int U>
-__device__ __forceinline__ void pass_cross(const PassShared& sh, const float2* xs, const float4* zd,
-                                           float2 (&aa)[16], float2 (&bb)[16]) {
+__device__ __forceinline__ void pass_cross(const PassShared& sh, const float2* xs, const float2* zs,
+                                           float2 (&acc)[16]) {
   constexpr int D = 1 << U, NBK = D / 4, NB = NBK * NBK;
   const int blk = threadIdx.x % NB, rg = threadIdx.x / NB, nrg = blockDim.x / NB;
   const int bi = blk / NBK, bk = blk % NBK;
@@ -269,22 +173,17 @@ __device__ __forceinline__ void pass_cross(const PassShared& sh, const float2* x
   }
   for (int r = rg; r < nrest; r += nrg) {
     const int ro = sh.rl[r];
-    float4 zv[4];
-    float2 xx[4];
+    float2 zz[4], xx[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      zv[i] = zd[wz[i] ^ ro];
+      const float2 v = zs[wz[i] ^ ro];
+      zz[i] = cf(v.x, -v.y);
       xx[i] = xs[wx[i] ^ ro];
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float2 zr = cf(zv[i].x, zv[i].y), zi = cf(zv[i].z, zv[i].w);
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        aa[i * 4 + k] = f2fma(zr, xx[k], aa[i * 4 + k]);
-        bb[i * 4 + k] = f2fma(zi, xx[k], bb[i * 4 + k]);
-      }
-    }
+      for (int k = 0; k < 4; ++k) acc[i * 4 + k] = fmac(acc[i * 4 + k], zz[i], xx[k]);
   }
 }
 
@@ -292,15 +191,14 @@ __device__ __forceinline__ void pass_cross(const PassShared& sh, const float2* x
 // chunk's partial (row-major 16 x 16 entries of M).  `red` aliases the tile
 // buffers.
 template <int U>
-__device__ __forceinline__ void pass_flush(const float2 (&aa)[16], const float2 (&bb)[16], double2* red,
-                                           double2* out) {
+__device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red, double2* out) {
   constexpr int D = 1 << U, NBK = D / 4, NB = NBK * NBK;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int blk = threadIdx.x % NB;
   __syncthreads();   // tile buffers free
 #pragma unroll
   for (int e = 0; e < 16; ++e) {
-    double re = (double)aa[e].x + (double)bb[e].y, im = (double)aa[e].y - (double)bb[e].x;
+    double re = (double)acc[e].x, im = (double)acc[e].y;
 #pragma unroll
     for (int o = NB; o < 32; o <<= 1) {
       re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -386,7 +284,7 @@ __device__ __forceinline__ int64_t next_in_mask(int64_t x, int64_t mask) { retur
 
 template <int U>
 __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& gd, const PassShared& sh, float2* xs,
-                                           float4* zd, int g, int b, int chunk, float2* psi, const float2* z_in,
+                                           float2* zs, int g, int b, int chunk, float2* psi, const float2* z_in,
                                            float2* z_out) {
   const int n = bd.n[b];
   const int64_t ntiles = (int64_t)1 << (n - sh.T);
@@ -394,46 +292,37 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
   float2* xv = psi + bd.vec_off[b];
   const float2* zv_in = z_in + bd.vec_off[b];
   float2* zv_out = z_out + bd.vec_off[b];
-  float2 aa[16], bb[16];
+  float2 acc[16];
 #pragma unroll
-  for (int e = 0; e < 16; ++e) aa[e] = bb[e] = cf(0.f, 0.f);
+  for (int e = 0; e < 16; ++e) acc[e] = cf(0.f, 0.f);
   const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
   const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
-  const int tsz = 1 << GT;   // buffer stride (tiles of small states use a prefix)
   int64_t base = deposit_bits(t0, rest_mask);
-  pass_issue(sh, xv + base, zv_in + base, xs, xs + tsz);
-  cp_async_commit();
   for (int64_t tt = t0; tt < t1; ++tt) {
-    const int cur = (int)((tt - t0) & 1);
-    float2* xb = xs + cur * 2 * tsz;
-    float2* zb = xb + tsz;
-    const int64_t nbase = next_in_mask(base, rest_mask);
-    if (tt + 1 < t1) {
-      float2* xn = xs + (cur ^ 1) * 2 * tsz;
-      pass_issue(sh, xv + nbase, zv_in + nbase, xn, xn + tsz);
-    }
+    pass_issue(sh, xv + base, zv_in + base, xs, zs);
     cp_async_commit();
-    cp_async_wait<1>();
+    cp_async_wait<0>();
     __syncthreads();
-    pass_apply<U>(sh, xb, zb, zd, g > 0);
+    if (g > 0) {
+      pass_apply<U>(sh, xs, zs);
+      __syncthreads();
+      pass_store(sh, xv + base, zv_out + base, xs, zs);
+    }
+    pass_cross<U>(sh, xs, zs, acc);
     __syncthreads();
-    if (g > 0) pass_store(sh, xv + base, zv_out + base, xb, zb);
-    pass_cross<U>(sh, xb, zd, aa, bb);
-    __syncthreads();
-    base = nbase;
+    base = next_in_mask(base, rest_mask);
   }
-  cp_async_wait<0>();
-  pass_flush<U>(aa, bb, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
+  pass_flush<U>(acc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS, 1) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
+__global__ void __launch_bounds__(BLOCK_THREADS, 2) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
                                                               const float2* z_in, float2* z_out,
                                                               const double2* gates, const double2* old_gates,
                                                               const signed char* arity, const int* nlayers,
                                                               const int* active) {
   extern __shared__ __align__(16) unsigned char dyn[];
-  float2* xs = reinterpret_cast<float2*>(dyn);   // buffer k: x at xs + 2k 2^GT, z right after
-  float4* zd = reinterpret_cast<float4*>(xs + 4 * (1 << GT));
+  float2* xs = reinterpret_cast<float2*>(dyn);
+  float2* zs = xs + (1 << GT);
   __shared__ PassShared sh;
   for (int chunk = blockIdx.x; chunk < gd.nchunks; chunk += gridDim.x) {
     const int b = gd.chunk_state[chunk];
@@ -513,16 +402,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1) k_group_pass(BatchDev bd, Gr
         const int r = e / m, c = e % m;
         const double2 vn = cconj(gates[bd.gate_off[b] + slot * 16 + c * m + r]);
         const double2 vo = cconj(old_gates[((int64_t)b * GMAXSTEPS + st) * 16 + c * m + r]);
-        sh.gr[1][st][e] = cf((float)vn.x, (float)vn.x);
-        sh.gi[1][st][e] = cf((float)vn.y, (float)vn.y);
-        sh.gr[0][st][e] = cf((float)vo.x, (float)vo.x);
-        sh.gi[0][st][e] = cf((float)vo.y, (float)vo.y);
+        sh.gm[1][st][e] = cf((float)vn.x, (float)vn.y);
+        sh.gm[0][st][e] = cf((float)vo.x, (float)vo.y);
       }
     }
     __syncthreads();
-    if (U == 4) pass_chunk<4>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
-    else if (U == 3) pass_chunk<3>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
-    else pass_chunk<2>(bd, gd, sh, xs, zd, g, b, chunk, psi, z_in, z_out);
+    if (U == 4) pass_chunk<4>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    else if (U == 3) pass_chunk<3>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    else pass_chunk<2>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
   }
 }
 
@@ -704,7 +591,7 @@ int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi
     if (e != cudaSuccess) return (int)e;
     attr_set = true;
   }
-  int grid = gd.nchunks < 152 ? gd.nchunks : 152;   // one block per SM
+  int grid = gd.nchunks < 2 * 152 ? gd.nchunks : 2 * 152;   // two blocks per SM
   if (grid < 1) grid = 1;
   qm_note_launch();
   k_group_pass<<<grid, BLOCK_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,

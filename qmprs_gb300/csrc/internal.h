@@ -98,7 +98,7 @@ struct GateSel {
 #define GW 4
 #define GM (1 << GW)
 #define GMM (GM * GM)
-#define GT 12
+#define GT 11
 #define GCHUNK 16
 #define GMAXSTEPS 8
 

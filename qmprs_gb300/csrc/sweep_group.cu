@@ -117,9 +117,12 @@ struct PassShared {
   float2 gm[2][GMAXSTEPS][16];   // [peel | new][step]: the applied matrix, row-major complex
 };
 
-// Dynamic shared memory: the tile of x and of z (float2 each).  Two blocks
-// share an SM, so one block's loads overlap the other's arithmetic.
+// Dynamic shared memory: the tile of x and of z (float2 each).  Four blocks
+// of four warps share an SM, so some blocks' loads overlap the others'
+// arithmetic.
 #define PASS_DYN_SMEM ((size_t)(2 * sizeof(float2)) * (1 << GT))
+#define PASS_THREADS 128
+#define PASS_BLOCKS_PER_SM 4
 
 // tile-local bit of global position p (p must be in pos_mask)
 __device__ __forceinline__ int tile_bit(int pos_mask, int p) { return __popc(pos_mask & ((1 << p) - 1)); }
@@ -230,11 +233,10 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Full tiles (2^GT amplitudes, BLOCK_THREADS threads): thread t handles
-// tile indices li = t + 256 u, whose offset is d0[t & 63] | d1[(t >> 6) + 4 u]
-// and whose swizzle is li ^ (((t >> 4) ^ u) & 15).
-#define PASS_PER ((1 << GT) / BLOCK_THREADS)
-static_assert(BLOCK_THREADS == 256 && GT == 12, "the full-tile index split assumes 256 threads and 2^12 tiles");
+// Full tiles (2^GT amplitudes): thread t handles tile indices
+// li = t + PASS_THREADS u, whose offset is d0[t & 63] | d1[(t >> 6) + u PASS_THREADS / 64].
+#define PASS_PER ((1 << GT) / PASS_THREADS)
+static_assert(PASS_THREADS % 64 == 0 && (1 << GT) % PASS_THREADS == 0, "full-tile index split");
 
 __device__ __forceinline__ void pass_issue(const PassShared& sh, const float2* xg, const float2* zg, float2* xs,
                                            float2* zs) {
@@ -242,9 +244,9 @@ __device__ __forceinline__ void pass_issue(const PassShared& sh, const float2* x
     const int t = threadIdx.x, lo = sh.d0[t & 63];
 #pragma unroll
     for (int u = 0; u < PASS_PER; ++u) {
-      const int li = t + u * BLOCK_THREADS;
-      const int o = lo | sh.d1[(t >> 6) + 4 * u];
-      const int sl = li ^ (((t >> 4) ^ u) & 15);
+      const int li = t + u * PASS_THREADS;
+      const int o = lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)];
+      const int sl = swz(li);
       cp_async8(xs + sl, xg + o);
       cp_async8(zs + sl, zg + o);
     }
@@ -263,9 +265,9 @@ __device__ __forceinline__ void pass_store(const PassShared& sh, float2* xg, flo
     const int t = threadIdx.x, lo = sh.d0[t & 63];
 #pragma unroll
     for (int u = 0; u < PASS_PER; ++u) {
-      const int li = t + u * BLOCK_THREADS;
-      const int o = lo | sh.d1[(t >> 6) + 4 * u];
-      const int sl = li ^ (((t >> 4) ^ u) & 15);
+      const int li = t + u * PASS_THREADS;
+      const int o = lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)];
+      const int sl = swz(li);
       xg[o] = xs[sl];
       zg[o] = zs[sl];
     }
@@ -315,7 +317,7 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
   pass_flush<U>(acc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS, 2) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
+__global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
                                                               const float2* z_in, float2* z_out,
                                                               const double2* gates, const double2* old_gates,
                                                               const signed char* arity, const int* nlayers,
@@ -591,10 +593,10 @@ int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi
     if (e != cudaSuccess) return (int)e;
     attr_set = true;
   }
-  int grid = gd.nchunks < 2 * 152 ? gd.nchunks : 2 * 152;   // two blocks per SM
+  int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
   if (grid < 1) grid = 1;
   qm_note_launch();
-  k_group_pass<<<grid, BLOCK_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,
+  k_group_pass<<<grid, PASS_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,
                                                           nlayers, active);
   return 0;
 }

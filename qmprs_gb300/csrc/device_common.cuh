@@ -162,3 +162,27 @@ __device__ __forceinline__ float2 fmac(float2 acc, float2 a, float2 b) {
   acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
   return acc;
 }
+
+// Compensated accumulation of exact products (double-float): p = u v is
+// split exactly into ph + pl (fma), ph enters (hi, lo) through a TwoSum and
+// pl and the TwoSum error land in lo.  Flushed to fp64 every TT_FLUSH rows,
+// the relative error of a Gram entry is about TT_FLUSH * 2^-48 of the sum of
+// |products|, far below the 1e-10 truncation cutoff the eigenvalues decide.
+struct DF {
+  float hi, lo;
+};
+
+// Every operation is an explicitly rounded intrinsic, so the compiler never
+// contracts the product into the sum (which would break the error terms).
+__device__ __forceinline__ void df_add_prod(DF& s, float u, float v) {
+  const float ph = __fmul_rn(u, v);
+  const float pl = __fmaf_rn(u, v, -ph);
+  const float t = __fadd_rn(s.hi, ph);
+  const float bv = __fsub_rn(t, s.hi);
+  const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, bv)), __fsub_rn(ph, bv));
+  s.lo = __fadd_rn(s.lo, __fadd_rn(err, pl));
+  s.hi = t;
+}
+
+// rows summed in double-float between fp64 flushes
+#define TT_FLUSH 32

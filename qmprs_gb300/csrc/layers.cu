@@ -5,27 +5,52 @@
 // form of the working state is its right-to-left truncated SVD, computed one
 // cut at a time.  Cut c of state b holds the remainder M (2^c x w, w = 2 r,
 // r = bond c+1, row-major, complex64).  k_layer_gram reduces its Gram matrix
-// in fp64, the last tile diagonalises it (Jacobi, fp64), applies quimb's
+// to fp64 (exact fp32 products, compensated sums), the last tile diagonalises it (Jacobi, fp64), applies quimb's
 // rsum2 cutoff with max_bond 2, fixes the singular-vector phases and stores
-// the site tensor; k_layer_project forms the next remainder M V.  After the
+// the site tensor; k_layer_project forms the next remainder M V.  The Gram
+// sums exact fp32 products in double-float and flushes to fp64.  After the
 // last cut, k_layer_build normalises site 0 and turns the n site tensors
 // into n gates (mps.py:565-847) in closed form.
 #include "device_common.cuh"
 
-// Gram rows of width W (2 or 4): products of fp32 inputs are exact in fp64.
+// Gram rows of width W (2 or 4): the upper triangle in double-float (exact
+// fp32 products, compensated sums), flushed to fp64 every TT_FLUSH rows and
+// mirrored into the lower triangle.
 template <int W>
 __device__ __forceinline__ void gram_rows(const float2* m, int64_t lo, int64_t hi, double (&acc)[32]) {
-  for (int64_t row = lo + threadIdx.x; row < hi; row += blockDim.x) {
-    double2 x[W];
+  constexpr int NE = W * (W + 1) / 2;
+  int64_t row = lo + threadIdx.x;
+  while (row < hi) {
+    DF re[NE], im[NE];
 #pragma unroll
-    for (int a = 0; a < W; ++a) x[a] = f2d(m[row * W + a]);
+    for (int k = 0; k < NE; ++k) re[k] = im[k] = DF{0.f, 0.f};
+    for (int f = 0; f < TT_FLUSH && row < hi; ++f, row += blockDim.x) {
+      float2 x[W];
+#pragma unroll
+      for (int a = 0; a < W; ++a) x[a] = m[row * W + a];
+      int k = 0;
+#pragma unroll
+      for (int a = 0; a < W; ++a)
+#pragma unroll
+        for (int e = a; e < W; ++e, ++k) {
+          df_add_prod(re[k], x[a].x, x[e].x);   // conj(x_a) x_e
+          df_add_prod(re[k], x[a].y, x[e].y);
+          df_add_prod(im[k], x[a].x, x[e].y);
+          df_add_prod(im[k], -x[a].y, x[e].x);
+        }
+    }
+    int k = 0;
 #pragma unroll
     for (int a = 0; a < W; ++a)
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        const double2 p = cmulc(x[a], x[e]);
-        acc[2 * (a * 4 + e)] += p.x;
-        acc[2 * (a * 4 + e) + 1] += p.y;
+      for (int e = a; e < W; ++e, ++k) {
+        const double sr = (double)re[k].hi + (double)re[k].lo, si = (double)im[k].hi + (double)im[k].lo;
+        acc[2 * (a * 4 + e)] += sr;
+        acc[2 * (a * 4 + e) + 1] += si;
+        if (e != a) {
+          acc[2 * (e * 4 + a)] += sr;
+          acc[2 * (e * 4 + a) + 1] -= si;
+        }
       }
   }
 }

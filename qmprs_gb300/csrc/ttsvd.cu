@@ -23,6 +23,7 @@
 #include "device_common.cuh"
 
 #define TT_CH 32
+#define TT_EIG_SMEM_W 64   // widest Gram diagonalised in shared memory (2 x 64 KB)
 
 __host__ __device__ inline int chi_eff(int chi, int n) {
   const int cap = 1 << (n / 2);
@@ -161,8 +162,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
   }
 }
 
-// One CTA per state; G (in place in `gram`) and V (`vwork`) are row-major
-// w x w in global memory.
+// One CTA per state; G and V are row-major w x w.  For w <= TT_EIG_SMEM_W
+// they live in shared memory (copied from `gram`, written back to `gram`
+// and `vwork` at the end), otherwise in place in global memory: each
+// Jacobi round is four block-wide phases, and shared memory takes the
+// memory latency out of them.
 __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step, int* bonds, double2* gram,
                                                           double2* vwork, int max_bond, double cutoff,
                                                           double2* vsel, double2* tensors, int chi) {
@@ -186,9 +190,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     return;
   }
   const int w = 2 * r;
-  double2* G = gram + (int64_t)b * WW;
-  double2* V = vwork + (int64_t)b * WW;
-  for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[e] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
+  extern __shared__ double2 eig_sm[];
+  double2* Gg = gram + (int64_t)b * WW;
+  double2* Vg = vwork + (int64_t)b * WW;
+  const bool in_smem = w <= TT_EIG_SMEM_W;
+  const int ld = in_smem ? w + 1 : w;   // padded rows: column walks hit distinct banks
+  double2* G = in_smem ? eig_sm : Gg;
+  double2* V = in_smem ? eig_sm + w * ld : Vg;
+  if (in_smem)
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) G[(e / w) * ld + e % w] = Gg[e];
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   const int half = w / 2;
   for (int sweep = 0; sweep < 40; ++sweep) {
@@ -201,9 +212,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
         int p = t1 == 0 ? 0 : 1 + ((t1 - 1 + k) % (w - 1));
         int q = 1 + ((t2 - 1 + k) % (w - 1));
         if (p > q) { const int tmp = p; p = q; q = tmp; }
-        const double2 g = G[p * w + q];
+        const double2 g = G[p * ld + q];
         const double ag = cabs_(g);
-        const double app = G[p * w + p].x, aqq = G[q * w + q].x;
+        const double app = G[p * ld + p].x, aqq = G[q * ld + q].x;
         const int rot = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)));
         s_p[i] = p;
         s_q[i] = q;
@@ -227,12 +238,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
         const int p = s_p[i], q = s_q[i];
         const double cc = s_c[i];
         const double2 se = s_se[i], sce = s_sce[i];
-        const double2 xp = G[row * w + p], xq = G[row * w + q];
-        G[row * w + p] = csub(cscale(xp, cc), cmul(sce, xq));
-        G[row * w + q] = cadd(cmul(se, xp), cscale(xq, cc));
-        const double2 vp = V[row * w + p], vq = V[row * w + q];
-        V[row * w + p] = csub(cscale(vp, cc), cmul(sce, vq));
-        V[row * w + q] = cadd(cmul(se, vp), cscale(vq, cc));
+        const double2 xp = G[row * ld + p], xq = G[row * ld + q];
+        G[row * ld + p] = csub(cscale(xp, cc), cmul(sce, xq));
+        G[row * ld + q] = cadd(cmul(se, xp), cscale(xq, cc));
+        const double2 vp = V[row * ld + p], vq = V[row * ld + q];
+        V[row * ld + p] = csub(cscale(vp, cc), cmul(sce, vq));
+        V[row * ld + q] = cadd(cmul(se, vp), cscale(vq, cc));
       }
       __syncthreads();
       for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
@@ -241,17 +252,17 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
         const int p = s_p[i], q = s_q[i];
         const double cc = s_c[i];
         const double2 se = s_se[i], sce = s_sce[i];
-        const double2 xp = G[p * w + col], xq = G[q * w + col];
-        G[p * w + col] = csub(cscale(xp, cc), cmul(se, xq));
-        G[q * w + col] = cadd(cmul(sce, xp), cscale(xq, cc));
+        const double2 xp = G[p * ld + col], xq = G[q * ld + col];
+        G[p * ld + col] = csub(cscale(xp, cc), cmul(se, xq));
+        G[q * ld + col] = cadd(cmul(sce, xp), cscale(xq, cc));
       }
       __syncthreads();
       if (threadIdx.x < half && s_flag[threadIdx.x]) {
         const int p = s_p[threadIdx.x], q = s_q[threadIdx.x];
-        G[p * w + q] = czero();
-        G[q * w + p] = czero();
-        G[p * w + p].y = 0.0;
-        G[q * w + q].y = 0.0;
+        G[p * ld + q] = czero();
+        G[q * ld + p] = czero();
+        G[p * ld + p].y = 0.0;
+        G[q * ld + q].y = 0.0;
       }
       __syncthreads();
     }
@@ -259,7 +270,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * w + i].x; }
+    for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * ld + i].x; }
     for (int i = 1; i < w; ++i) {
       const int kk = s_perm[i];
       const double key = s_lam[i];
@@ -276,18 +287,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   }
   __syncthreads();
   const int keep = s_keep;
-  if (threadIdx.x < keep) phase_fix_column(V, w, w, s_perm[threadIdx.x]);
+  if (threadIdx.x < keep) phase_fix_column(V, w, ld, s_perm[threadIdx.x]);
   __syncthreads();
   double2* vs = vsel + (int64_t)b * WW;
   for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
     const int a = e / keep, col = e % keep;
-    vs[a * TT_MAXB + col] = V[a * w + s_perm[col]];
+    vs[a * TT_MAXB + col] = V[a * ld + s_perm[col]];
   }
   const int ce = chi_eff(chi, n);
   double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
   for (int e = threadIdx.x; e < keep * 2 * r; e += blockDim.x) {
     const int l = e / (2 * r), pr = e % (2 * r);   // e = l * 2r + (p * r + rr)
-    ts[e] = cconj(V[pr * w + s_perm[l]]);
+    ts[e] = cconj(V[pr * ld + s_perm[l]]);
   }
 }
 
@@ -392,6 +403,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_mps_contract(BatchDev bd, int
   }
 }
 
+#define TT_EIG_SMEM ((size_t)2 * TT_EIG_SMEM_W * (TT_EIG_SMEM_W + 1) * sizeof(double2))
+
 static int grid_for(const BatchDev& bd) {
   int g = bd.ntiles;
   const int cap = 152 * 8;
@@ -406,8 +419,14 @@ void launch_tt_gram(const BatchDev& bd, int step, const float2* sv, const float2
 
 void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, double2* vwork, int max_bond,
                    double cutoff, double2* vsel, double2* tensors, int chi, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_tt_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_EIG_SMEM);
+    attr = true;
+  }
   qm_note_launch();
-  k_tt_eig<<<bd.B, BLOCK_THREADS, 0, s>>>(bd, step, bonds, gram, vwork, max_bond, cutoff, vsel, tensors, chi);
+  k_tt_eig<<<bd.B, BLOCK_THREADS, TT_EIG_SMEM, s>>>(bd, step, bonds, gram, vwork, max_bond, cutoff, vsel, tensors,
+                                                    chi);
 }
 
 void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const float2* src, float2* dst,

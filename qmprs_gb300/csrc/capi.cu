@@ -45,8 +45,8 @@ struct qmprs_plan {
   // grouped sweep: chunk tables, group plan, replaced gates, chunk partials
   int nchunks = 0;
   int *d_chunk_state = nullptr, *d_chunk_idx = nullptr, *d_state_chunk0 = nullptr, *d_state_nchunks = nullptr,
-      *d_ngroups = nullptr;
-  GroupEnt* d_grp = nullptr;
+      *d_ngroups = nullptr, *d_nrgroups = nullptr;
+  GroupEnt *d_grp = nullptr, *d_rgrp = nullptr;
   double2 *d_old_gates = nullptr, *d_gpartials = nullptr;
   GroupDev gd;
   // profiling of the sweep kernels (kernel classes: 0 environment stream,
@@ -235,7 +235,8 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->tt_partials, p->gram,      p->vsel,       p->vsel2,         p->site_t, p->vwork,
                   p->bonds,    p->active,       p->nlayers,    p->num_active,    p->nuc,
                   p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
-                  p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials};
+                  p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials,
+                  p->d_rgrp,   p->d_nrgroups};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -360,6 +361,8 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   PC(dalloc(&p->d_state_nchunks, B));
   PC(dalloc(&p->d_ngroups, B));
   PC(dalloc(&p->d_grp, (int64_t)B * gmax));
+  PC(dalloc(&p->d_rgrp, (int64_t)B * gmax));
+  PC(dalloc(&p->d_nrgroups, B));
   PC(dalloc(&p->d_old_gates, (int64_t)B * GMAXSTEPS * 16));
   PC(dalloc(&p->d_gpartials, (int64_t)p->nchunks * GMM));
   PC(cudaMemcpy(p->d_chunk_state, chunk_state.data(), sizeof(int) * p->nchunks, cudaMemcpyHostToDevice));
@@ -379,6 +382,8 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   gd.ngroups = p->d_ngroups;
   gd.old_gates = p->d_old_gates;
   gd.partials = p->d_gpartials;
+  gd.rgrp = p->d_rgrp;
+  gd.nrgroups = p->d_nrgroups;
   BatchDev& bd = p->bd;
   bd.B = B;
   bd.ntiles = p->ntiles;
@@ -537,11 +542,15 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   // group plan of the backward order (the gates' arity does not change
   // between sweeps)
   launch_group_plan(p->bd, p->gd, ar, num_layers, s);
-  std::vector<int> ngroups(p->B, 0);
+  std::vector<int> ngroups(p->B, 0), nrgroups(p->B, 0);
   CK(cudaMemcpyAsync(ngroups.data(), p->d_ngroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(nrgroups.data(), p->d_nrgroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  int max_groups = 0;
-  for (int b = 0; b < p->B; ++b) max_groups = std::max(max_groups, ngroups[b]);
+  int max_groups = 0, max_rpasses = 0;
+  for (int b = 0; b < p->B; ++b) {
+    max_groups = std::max(max_groups, ngroups[b]);
+    max_rpasses = std::max(max_rpasses, (nrgroups[b] + 1) / 2);
+  }
   float2* psi = p->S0;
   float2* t = p->S1;
   ProfLog log;
@@ -550,23 +559,23 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   for (int sw = 0; sw < num_sweeps; ++sw) {
     // algorithmic bytes per rebuild pass / group pass, counted from the
     // states active in this sweep
-    std::vector<double> amp_at(prof ? max_gates : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
+    std::vector<double> amp_rb(prof ? max_rpasses : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
     if (prof) {
       CK(cudaMemcpyAsync(act.data(), p->active, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       for (int b = 0; b < p->B; ++b)
         if (act[b]) {
-          for (int j = 0; j < p->gates_per_state[b]; ++j) amp_at[j] += (double)ipow2(p->n[b]);
+          for (int r = 0; r < (nrgroups[b] + 1) / 2; ++r) amp_rb[r] += (double)ipow2(p->n[b]);
           for (int g = 0; g < ngroups[b]; ++g) amp_grp[g] += (double)ipow2(p->n[b]);
         }
     }
-    // C|0>: three consecutive gates per pass on 4-qubit windows
+    // C|0>: two 4-qubit windows of consecutive gates per pass
     launch_set_zero_state(p->bd, psi, p->active, s);
-    for (int j = 0; j < max_gates; j += 3) {
+    for (int r = 0; r < max_rpasses; ++r) {
       log.begin(prof, s);
-      launch_rebuild_win(p->bd, psi, gates, ar, num_layers, p->active, j, 3, s);
+      launch_rebuild_pass(p->bd, p->gd, r, psi, gates, ar, num_layers, p->active, s);
       log.end(prof, 2, s);
-      if (prof) p->prof_bytes[2] += 16.0 * amp_at[j];
+      if (prof) p->prof_bytes[2] += 16.0 * amp_rb[r];
     }
     // backward sweep by groups: the pass applies group g-1's peels to psi
     // and its new gates to t (the target itself for g = 1) and reduces the
@@ -604,20 +613,19 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
   int max_gates = 0;
   int rc = read_max_gates(p, num_layers, s, &max_gates);
   if (rc != QMPRS_OK) return rc;
+  const signed char* ar = (const signed char*)arity;
+  // C|0> with the rebuild passes of the sweep: two 4-qubit windows of
+  // consecutive gates per pass
+  launch_group_plan(p->bd, p->gd, ar, num_layers, s);
+  std::vector<int> nrgroups(p->B, 0);
+  CK(cudaMemcpyAsync(nrgroups.data(), p->d_nrgroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int passes = 0;
+  for (int b = 0; b < p->B; ++b) passes = std::max(passes, (nrgroups[b] + 1) / 2);
   float2* psi = (float2*)out;
   launch_set_zero_state(p->bd, psi, nullptr, s);
-  GateSel sel;
-  sel.mode = SEL_REBUILD;
-  sel.layer = 0;
-  sel.adjoint = 0;
-  sel.gates = (const double2*)gates;
-  sel.arity = (const signed char*)arity;
-  sel.nlayers = num_layers;
-  sel.active = nullptr;
-  for (int j = 0; j < max_gates; ++j) {
-    sel.step = j;
-    launch_apply_gate(p->bd, psi, sel, s);
-  }
+  for (int r = 0; r < passes; ++r)
+    launch_rebuild_pass(p->bd, p->gd, r, psi, (const double2*)gates, ar, num_layers, nullptr, s);
   CK(cudaGetLastError());
   return QMPRS_OK;
 }

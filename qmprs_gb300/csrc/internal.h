@@ -120,6 +120,8 @@ struct GroupDev {
   int* ngroups;              // [B]
   double2* old_gates;        // [B * GMAXSTEPS * 16] gates replaced by the last group
   double2* partials;         // [nchunks * GMM]
+  GroupEnt* rgrp;            // [B * gmax] forward-order groups (circuit rebuild)
+  int* nrgroups;             // [B]
 };
 
 // ---- launches (defined in the .cu files) ---------------------------------
@@ -145,10 +147,10 @@ void launch_layer_fidelity(const BatchDev& bd, int layer, const float2* work, in
                            cudaStream_t s);
 
 // (d) sweep
-void launch_rebuild_win(const BatchDev& bd, float2* psi, const double2* gates, const signed char* arity,
-                        const int* nlayers, const int* active, int j0, int count, cudaStream_t s);
 void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, const int* nlayers,
                        cudaStream_t s);
+void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
+                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s);
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
                       const double2* gates, const signed char* arity, const int* nlayers, const int* active,
                       cudaStream_t s);

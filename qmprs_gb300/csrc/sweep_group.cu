@@ -44,6 +44,23 @@ __device__ __forceinline__ bool bwd_step(const BatchDev& bd, const signed char* 
   return (*k == 1) || (*k == 2 && s <= n - 2);
 }
 
+// Gate of state b at forward (circuit-order) position j: generated layer
+// L - 1 - j / n, site j % n.
+__device__ __forceinline__ bool fwd_step(const BatchDev& bd, const signed char* arity, int L, int n, int b, int j,
+                                         int64_t* slot, int* q, int* k) {
+  if (j < 0 || j >= L * n) return false;
+  const int l = L - 1 - j / n, s = j % n;
+  *slot = (int64_t)l * n + s;
+  *q = s;
+  *k = arity[bd.gate_off[b] / 16 + *slot];
+  return (*k == 1) || (*k == 2 && s <= n - 2);
+}
+
+__device__ __forceinline__ bool step_gate(bool forward, const BatchDev& bd, const signed char* arity, int L, int n,
+                                          int b, int j, int64_t* slot, int* q, int* k) {
+  return forward ? fwd_step(bd, arity, L, n, b, j, slot, q, k) : bwd_step(bd, arity, L, n, b, j, slot, q, k);
+}
+
 // Place the low bits of v, in order, at the set bits of mask (ascending).
 __device__ __forceinline__ int64_t deposit_bits(int64_t v, int64_t mask) {
   int64_t r = 0;
@@ -65,7 +82,10 @@ __device__ __forceinline__ int swz(int li) { return li ^ (((li >> 4) ^ (li >> 8)
 
 // ---- group plan --------------------------------------------------------------
 
-__global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers) {
+// Groups of consecutive steps (backward sweep order, or the forward circuit
+// order when `forward`) whose qubits fit a window of min(GW, n) qubits.
+__global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers, int forward,
+                             GroupEnt* grp, int* ngroups) {
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bd.B; b += gridDim.x * blockDim.x) {
     const int n = bd.n[b], L = nlayers[b], total = L * n;
     const int u = n < GW ? n : GW;
@@ -73,7 +93,7 @@ __global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity,
     while (j < total) {
       int64_t slot;
       int q, k;
-      if (!bwd_step(bd, arity, L, n, b, j, &slot, &q, &k)) {
+      if (!step_gate(forward, bd, arity, L, n, b, j, &slot, &q, &k)) {
         atomicOr(bd.err, KERR_BAD_GATE);   // skipped, as the per-gate launches do
         ++j;
         continue;
@@ -81,7 +101,7 @@ __global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity,
       int mask = (k == 2 ? 3 : 1) << q;
       const int j0 = j++;
       while (j < total && j - j0 < GMAXSTEPS) {
-        if (!bwd_step(bd, arity, L, n, b, j, &slot, &q, &k)) break;
+        if (!step_gate(forward, bd, arity, L, n, b, j, &slot, &q, &k)) break;
         const int m2 = mask | ((k == 2 ? 3 : 1) << q);
         if (__popc(m2) > u) break;
         mask = m2;
@@ -94,11 +114,11 @@ __global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity,
         e.cnt = j - j0;
         e.qmask = mask;
         e.u = u;
-        gd.grp[(int64_t)b * gd.gmax + ng] = e;
+        grp[(int64_t)b * gd.gmax + ng] = e;
         ++ng;
       }
     }
-    gd.ngroups[b] = ng;
+    ngroups[b] = ng;
   }
 }
 
@@ -415,6 +435,157 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
   }
 }
 
+// ---- circuit rebuild ---------------------------------------------------------------
+
+// C|0> before each sweep (reference qmprs/synthesis/mps_encoding/sequential.py:
+// 443-447 densifies the circuit): the forward gate order cut into groups
+// that fit a 4-qubit window (three consecutive gates); pass p applies
+// forward groups 2p and 2p + 1 to a shared-memory tile holding both windows,
+// so one read and one write of the state serve up to six gates.
+struct RebuildShared {
+  int pos_mask, T, nw;
+  int wm[2];                       // tile-local masks of the two windows
+  int nst[2];
+  int pk[2][GMAXSTEPS], phi[2][GMAXSTEPS], plo[2][GMAXSTEPS];
+  int wl[2][GM];                   // window index -> swizzled tile offset
+  int pl[2][1 << (GT - GW)];       // position -> swizzled tile offset
+  int d0[64], d1[64];
+  float2 gm[2][GMAXSTEPS][16];     // the gates, row-major complex
+};
+
+template <int U>
+__device__ __forceinline__ void rebuild_apply(const RebuildShared& sh, int w, float2* xs) {
+  const int npos = 1 << (sh.T - U);
+  for (int p = threadIdx.x; p < npos; p += blockDim.x) {
+    const int po = sh.pl[w][p];
+    float2 a[1 << U];
+#pragma unroll
+    for (int i = 0; i < (1 << U); ++i) a[i] = xs[po ^ sh.wl[w][i]];
+    for (int s = 0; s < sh.nst[w]; ++s)
+      if (sh.pk[w][s]) win_apply<U>(a, sh.gm[w][s], sh.pk[w][s], sh.phi[w][s], sh.plo[w][s]);
+#pragma unroll
+    for (int i = 0; i < (1 << U); ++i) xs[po ^ sh.wl[w][i]] = a[i];
+  }
+}
+
+template <int U>
+__device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev& gd, const RebuildShared& sh,
+                                              float2* xs, int b, int chunk, float2* psi) {
+  const int n = bd.n[b];
+  const int64_t ntiles = (int64_t)1 << (n - sh.T);
+  const int64_t rest_mask = (((int64_t)1 << n) - 1) & ~(int64_t)sh.pos_mask;
+  float2* xv = psi + bd.vec_off[b];
+  const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
+  const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
+  int64_t base = deposit_bits(t0, rest_mask);
+  for (int64_t tt = t0; tt < t1; ++tt) {
+    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x)
+      cp_async8(xs + swz(li), xv + base + (sh.d0[li & 63] | sh.d1[li >> 6]));
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int w = 0; w < sh.nw; ++w) {
+      rebuild_apply<U>(sh, w, xs);
+      __syncthreads();
+    }
+    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x)
+      xv[base + (sh.d0[li & 63] | sh.d1[li >> 6])] = xs[swz(li)];
+    __syncthreads();
+    base = next_in_mask(base, rest_mask);
+  }
+}
+
+__global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pass(BatchDev bd, GroupDev gd,
+                                                                                 int pass, float2* psi,
+                                                                                 const double2* gates,
+                                                                                 const signed char* arity,
+                                                                                 const int* nlayers,
+                                                                                 const int* active) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  float2* xs = reinterpret_cast<float2*>(dyn);
+  __shared__ RebuildShared sh;
+  for (int chunk = blockIdx.x; chunk < gd.nchunks; chunk += gridDim.x) {
+    const int b = gd.chunk_state[chunk];
+    if (active && !active[b]) continue;
+    const int ng = gd.nrgroups[b];
+    const int ga = 2 * pass;
+    if (ga >= ng) continue;
+    const int n = bd.n[b];
+    const int L = nlayers[b];
+    const int nw = ga + 1 < ng ? 2 : 1;
+    GroupEnt ge[2];
+    ge[0] = gd.rgrp[(int64_t)b * gd.gmax + ga];
+    ge[1] = nw == 2 ? gd.rgrp[(int64_t)b * gd.gmax + ga + 1] : ge[0];
+    const int T = n < GT ? n : GT;
+    const int U = ge[0].u;
+    __syncthreads();   // previous chunk done with the tables
+    if (threadIdx.x < 2 * GMAXSTEPS) {
+      const int w = threadIdx.x / GMAXSTEPS, st = threadIdx.x % GMAXSTEPS;
+      int64_t slot;
+      int q, k;
+      if (w < nw && st < ge[w].cnt && fwd_step(bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k)) {
+        sh.pk[w][st] = k;
+        sh.phi[w][st] = __popc(ge[w].qmask >> (q + 1));
+        sh.plo[w][st] = k == 2 ? __popc(ge[w].qmask >> (q + 2)) : 0;
+      } else {
+        sh.pk[w][st] = 0;
+      }
+    }
+    if (threadIdx.x == 0) {
+      int pm = 0;
+      const int qm = ge[0].qmask | ge[1].qmask;
+      for (int q = 0; q < n; ++q)
+        if ((qm >> q) & 1) pm |= 1 << (n - 1 - q);
+      for (int p = 0; p < n && __popc(pm) < T; ++p) pm |= 1 << p;
+      for (int w = 0; w < 2; ++w) {
+        int m = 0;
+        for (int q = 0; q < n; ++q)
+          if ((ge[w].qmask >> q) & 1) m |= 1 << tile_bit(pm, n - 1 - q);
+        sh.wm[w] = m;
+        sh.nst[w] = ge[w].cnt < GMAXSTEPS ? ge[w].cnt : GMAXSTEPS;
+      }
+      sh.pos_mask = pm;
+      sh.T = T;
+      sh.nw = nw;
+    }
+    __syncthreads();
+    const int full = (1 << T) - 1;
+    {
+      int lo6 = 0, m = sh.pos_mask;
+      for (int i = 0; i < 6 && m; ++i) {
+        lo6 |= m & (-m);
+        m &= m - 1;
+      }
+      for (int j = threadIdx.x; j < 64; j += blockDim.x) {
+        sh.d0[j] = deposit32(j, lo6);
+        sh.d1[j] = deposit32(j, m);
+      }
+    }
+    for (int t = threadIdx.x; t < 2 * (1 << U); t += blockDim.x) {
+      const int w = t >> U, a = t & ((1 << U) - 1);
+      sh.wl[w][a] = swz(deposit32(a, sh.wm[w]));
+    }
+    for (int t = threadIdx.x; t < 2 * (1 << (T - U)); t += blockDim.x) {
+      const int w = t / (1 << (T - U)), r = t % (1 << (T - U));
+      sh.pl[w][r] = swz(deposit32(r, full & ~sh.wm[w]));
+    }
+    for (int t = threadIdx.x; t < 2 * GMAXSTEPS * 16; t += blockDim.x) {
+      const int w = t / (GMAXSTEPS * 16), st = (t / 16) % GMAXSTEPS, e = t % 16;
+      int64_t slot;
+      int q, k;
+      if (w >= nw || st >= ge[w].cnt || !fwd_step(bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k)) continue;
+      const int m = 1 << k;
+      if (e >= m * m) continue;
+      const double2 v = gates[bd.gate_off[b] + slot * 16 + e];
+      sh.gm[w][st][e] = cf((float)v.x, (float)v.y);
+    }
+    __syncthreads();
+    if (U == 4) rebuild_chunk<4>(bd, gd, sh, xs, b, chunk, psi);
+    else if (U == 3) rebuild_chunk<3>(bd, gd, sh, xs, b, chunk, psi);
+    else rebuild_chunk<2>(bd, gd, sh, xs, b, chunk, psi);
+  }
+}
+
 // ---- per-group polar kernel ------------------------------------------------------
 
 // M <- G^T M on the rows of gate bits (h, l): the target-side update z <- P z
@@ -578,9 +749,20 @@ __global__ void __launch_bounds__(POLAR_THREADS) k_group_polar(BatchDev bd, Grou
 
 void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, const int* nlayers,
                        cudaStream_t s) {
-  qm_note_launch();
   const int blocks = (bd.B + 127) / 128;
-  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers);
+  qm_note_launch();
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, 0, gd.grp, gd.ngroups);
+  qm_note_launch();
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, 1, gd.rgrp, gd.nrgroups);
+}
+
+void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
+                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s) {
+  int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
+  if (grid < 1) grid = 1;
+  qm_note_launch();
+  k_rebuild_pass<<<grid, PASS_THREADS, (size_t)sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
+                                                                          nlayers, active);
 }
 
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,

@@ -315,6 +315,33 @@ def sweep(target: np.ndarray, n: int, layers: list[Layer], mode: str = "canonica
     return layers, nuc / float(np.linalg.norm(target))
 
 
+def iter_dioall(target: np.ndarray, n: int, num_layers: int, sweeps_per_layer: int,
+                mode: str = "canonical") -> tuple[list[Layer], list[list[float]]]:
+    """Iter-DiOall schedule (arXiv:2209.00595; the reference documents it as
+    the intended use of its sweep, sequential.py:410-433, without
+    implementing it): k = 1..num_layers, disentangle one more layer from the
+    residual C^H |target> (the newest layer is applied first in the
+    circuit), then sweep all layers ``sweeps_per_layer`` times.  No early
+    exit.  Returns the layers (circuit order) and the per-step lists of sweep
+    fidelities."""
+    t = target / np.linalg.norm(target)
+    layers: list[Layer] = []            # circuit order
+    fids: list[list[float]] = []
+    residual = t.copy()
+    for _ in range(num_layers):
+        layer, _ = generate_layer(residual, n, mode)
+        layers = [layer] + layers
+        step = []
+        for _ in range(sweeps_per_layer):
+            layers, f = sweep(t, n, layers, mode)
+            step.append(f)
+        fids.append(step)
+        residual = t.copy()
+        for lay in reversed(layers):    # C^H t: the last-applied layer's inverse first
+            residual = apply_inverse_layer(residual, n, lay)
+    return layers, fids
+
+
 @dataclass
 class EncodeResult:
     layers: list

@@ -301,6 +301,58 @@ class Engine:
         counts = torch.tensor([2 ** (n + 1) for n in ns], dtype=torch.int64, device="cuda")
         return vec * torch.repeat_interleave(inv, counts)
 
+    def encode_iterative(self, statevectors, bond_dimension: int, num_layers: int, sweeps_per_layer: int,
+                         nqubits=None) -> BatchResult:
+        """Iter-DiOall schedule (arXiv:2209.00595, documented by the
+        reference at qmprs/synthesis/mps_encoding/sequential.py:410-433):
+        for k = 1..num_layers, generate one analytic layer from the residual
+        C^H |target> of the current circuit (the newest layer is applied
+        first), then sweep all k layers `sweeps_per_layer` times.  Every state
+        gets all num_layers layers (no early exit).  ``sweep_fidelities``
+        holds the fidelity after every sweep, num_layers * sweeps_per_layer
+        columns."""
+        if nqubits is None:
+            p, sv = self.upload(statevectors, num_layers, bond_dimension)
+        else:
+            p = self.plan(nqubits, num_layers, bond_dimension)
+            sv = statevectors if statevectors.is_cuda else statevectors.to("cuda", non_blocking=True)
+        _, _, target = self.stage_mps(p, sv, bond_dimension)
+        B, L, S = p.B, int(num_layers), int(sweeps_per_layer)
+        gates = torch.zeros(p.gate_elems * 2, dtype=torch.float64, device="cuda")
+        arity = torch.zeros(p.gate_elems // 16, dtype=torch.int8, device="cuda")
+        nl = torch.zeros(B, dtype=torch.int32, device="cuda")
+        # gate-store rows (16 complex each) of generated layer l, all states
+        rows = [np.concatenate([p.gate_off[b] // 16 + l * n + np.arange(n) for b, n in enumerate(p.nqubits)])
+                for l in range(L)]
+        g_rows = gates.view(-1, 32)
+        fids = []
+        residual = target.clone()
+        for k in range(L):
+            g1, a1, _, _ = self.stage_layers(p, residual, 1, 1.0)
+            src = torch.as_tensor(rows[0], device="cuda")
+            dst = torch.as_tensor(rows[k], device="cuda")
+            g_rows[dst] = g1.view(-1, 32)[src]
+            arity[dst] = a1[src]
+            nl.fill_(k + 1)
+            if S > 0:
+                sf, _ = self.stage_sweeps(p, target, gates, arity, nl, S, 0.0)
+                fids.append(sf[: B * S].view(B, S))
+            residual = target.clone()
+            for l in range(k + 1):       # C^H t: inverse of generated layer 0 (applied last) first
+                self.apply_layer(p, residual, gates, arity, l, True)
+        circ = self.stage_circuit(p, gates, arity, nl)
+        ov = self.overlap(p, circ, sv)
+        nn = self.overlap(p, sv, sv)
+        torch.cuda.current_stream().synchronize()
+        ovh = ov.cpu().numpy().view(np.complex128)
+        nnh = nn.cpu().numpy().view(np.complex128).real
+        sfh = torch.cat(fids, dim=1).cpu().numpy() if fids else np.zeros((B, 0))
+        return BatchResult(
+            nqubits=p.nqubits, gates=gates.cpu().numpy().view(np.complex128), arity=arity.cpu().numpy(),
+            num_layers=nl.cpu().numpy(), layer_fidelities=np.zeros((B, L), np.complex128),
+            sweep_fidelities=sfh, sweeps_done=np.full(B, L * S, np.int32), fidelity=np.abs(ovh) / np.sqrt(nnh),
+            gate_off=p.gate_off, max_n=p.max_n, max_bond=int(bond_dimension))
+
     def _fallback(self, p: Plan, target, sv, analytic, gates, arity, nl, sf, sd, ov, nn, num_sweeps: int,
                   stop_fidelity: float):
         """States of a warm-started batch that end below stop_fidelity are

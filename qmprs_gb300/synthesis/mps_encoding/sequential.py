@@ -148,7 +148,8 @@ class Sequential(MPSEncoder):
 
     # ---- batched extension -------------------------------------------------------------
     def prepare_states(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
-                       stop_fidelity: float = 0.0, emit: bool = True, nqubits=None, *, warm_start=None):
+                       stop_fidelity: float = 0.0, emit: bool = True, nqubits=None, *, warm_start=None,
+                       schedule: str = "oall"):
         """Encode many statevectors at once (any mix of qubit counts).
 
         Same result per state as ``prepare_state`` (default
@@ -162,7 +163,13 @@ class Sequential(MPSEncoder):
         ``warm_start`` (keyword only; a ``qmprs_gb300.warmstart.WarmStartMLP``)
         starts the sweeps from the network's predicted layers; states that
         end below ``stop_fidelity`` fall back to the analytic layers.
+        ``schedule`` (keyword only): ``"oall"`` (the reference's: all layers,
+        then ``num_sweeps`` sweeps) or ``"iter_dioall"`` (one layer at a time
+        from the residual, each followed by ``num_sweeps`` sweeps of all
+        layers; arXiv:2209.00595, documented by the reference's sweep).
         """
+        if schedule not in ("oall", "iter_dioall"):
+            raise ValueError("schedule must be 'oall' or 'iter_dioall'.")
         if not isinstance(num_layers, int) or num_layers < 1:
             raise ValueError("The number of layers must be a positive integer.")
         if not isinstance(bond_dimension, int) or bond_dimension < 1:
@@ -172,15 +179,21 @@ class Sequential(MPSEncoder):
             ns = [int(n) for n in nqubits]
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
-            res = eng.encode(statevectors, bond_dimension, num_layers, num_sweeps, self.fidelity_threshold,
-                             stop_fidelity, nqubits=ns, warm_start=warm_start)
+            if schedule == "iter_dioall":
+                res = eng.encode_iterative(statevectors, bond_dimension, num_layers, num_sweeps, nqubits=ns)
+            else:
+                res = eng.encode(statevectors, bond_dimension, num_layers, num_sweeps, self.fidelity_threshold,
+                                 stop_fidelity, nqubits=ns, warm_start=warm_start)
         else:
             kets = [sv if isinstance(sv, Ket) else Ket(sv) for sv in statevectors]
             ns = [k.num_qubits for k in kets]
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
-            res = eng.encode([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
-                             self.fidelity_threshold, stop_fidelity, warm_start=warm_start)
+            if schedule == "iter_dioall":
+                res = eng.encode_iterative([k.data for k in kets], bond_dimension, num_layers, num_sweeps)
+            else:
+                res = eng.encode([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
+                                 self.fidelity_threshold, stop_fidelity, warm_start=warm_start)
         circuits = None
         if emit:
             circuits = []

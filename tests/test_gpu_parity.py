@@ -110,6 +110,23 @@ def test_sweeps_match_oracle(eng, ns, L, S_):
         assert abs(res.fidelity[b] - abs(np.vdot(psi, sv))) < FID_TOL
 
 
+@pytest.mark.parametrize("ns,L,S_", [([6, 7], 3, 2), ([8, 5], 2, 3)])
+def test_iter_dioall_matches_oracle(eng, ns, L, S_):
+    """Iter-DiOall schedule: every sweep fidelity of every step, and the
+    final overlap, against the oracle's restatement."""
+    svs = _svs(ns, 31)
+    res = eng.encode_iterative(svs, 64, L, S_)
+    assert res.sweep_fidelities.shape == (len(ns), L * S_)
+    for b, sv in enumerate(svs):
+        n = ns[b]
+        t = _oracle_target(sv, 64)
+        layers, fids = D.iter_dioall(t, n, L, S_)
+        flat = [f for step in fids for f in step]
+        assert np.allclose(res.sweep_fidelities[b], flat, atol=FID_TOL), (res.sweep_fidelities[b], flat)
+        psi = D.circuit_state(layers, n)
+        assert abs(res.fidelity[b] - abs(np.vdot(psi, sv))) < FID_TOL
+
+
 def test_sweeps_from_given_layers(eng):
     """_optimize_unitary_layers on oracle-made layers reproduces the oracle sweeps."""
     from qmprs_gb300.primitives import MPS

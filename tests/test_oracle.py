@@ -170,3 +170,17 @@ def test_readme_fidelity_n10_statistically():
     must fall in the same band."""
     f = [D.prepare_state(_rand_state(10, s), 512, 15, 50).fidelity for s in range(3)]
     assert 0.975 < float(np.mean(f)) < 0.995, f
+
+
+def test_iter_dioall_oracle_sweeps_never_lose_fidelity():
+    """Within each step of the Iter-DiOall schedule the sweeps do not lower
+    the fidelity, and the last one is the circuit's overlap."""
+    from oracle import states as S
+    n = 6
+    sv = S.random_mps(n, 4, 3)
+    t = sv / np.linalg.norm(sv)
+    layers, fids = D.iter_dioall(t, n, 3, 3)
+    for step in fids:
+        assert all(b >= a - 1e-12 for a, b in zip(step, step[1:]))
+    psi = D.circuit_state(layers, n)
+    assert abs(abs(np.vdot(psi, t)) - fids[-1][-1]) < 1e-10

@@ -205,6 +205,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def replica_spec(workload: str, states: int, seed: int, rank: int):
+    """The batch of one replica: every rank encodes its own seeded batch of
+    the same configuration (the path does not shard within a state)."""
+    return workload_spec(workload, states, seed + rank)
+
+
+def max_over_ranks(vals, world: int, device: str):
+    """Element-wise maximum over the ranks (a no-op for one rank)."""
+    import torch
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -214,7 +230,7 @@ def run_gpu(args, rank, world):
 
     local = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
-    ns, bonds, cfg, desc = workload_spec(args.workload, args.states, args.seed + rank)
+    ns, bonds, cfg, desc = replica_spec(args.workload, args.states, args.seed, rank)
     eng = E.engine()
     sv_dev = eng.random_mps_states(ns, bonds, seed=args.seed + 17 * rank)
     host = torch.empty(sv_dev.numel(), dtype=torch.float32, pin_memory=True)
@@ -298,10 +314,7 @@ def run_gpu(args, rank, world):
     achieved = (by_env / n_env) / (ms_env / n_env * 1e-3) / 1e9 if n_env and ms_env > 0 else 0.0
 
     # ---- max over ranks
-    t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms = float(t[0]), float(t[1])
+    ms, e2e_ms = max_over_ranks([ms, e2e_ms], world, "cuda")
     if rank != 0:
         return
     cores = len(os.sched_getaffinity(0))

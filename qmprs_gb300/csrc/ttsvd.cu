@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   __shared__ double2 s_se[TT_MAXW / 2], s_sce[TT_MAXW / 2];
   __shared__ int s_p[TT_MAXW / 2], s_q[TT_MAXW / 2], s_flag[TT_MAXW / 2];
   __shared__ int s_rot;
+  __shared__ double s_floor;
   __shared__ double s_lam[TT_MAXW];
   __shared__ int s_perm[TT_MAXW];
   __shared__ int s_keep;
@@ -202,6 +203,17 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   const int half = w / 2;
+  // Absolute rotation floor: off-diagonals at most 1e-15 of the trace move
+  // no eigenvalue by more than that (five orders below the 1e-10
+  // truncation cutoff).  Without it the rounding-level null-space block of
+  // a rank-deficient Gram keeps rotating until the sweep limit.
+  if (threadIdx.x == 0) {
+    double tr = 0.0;
+    for (int i = 0; i < w; ++i) tr += fabs(G[i * ld + i].x);
+    s_floor = 1e-15 * tr;
+  }
+  __syncthreads();
+  const double floor_abs = s_floor;
   for (int sweep = 0; sweep < 40; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
     __syncthreads();
@@ -215,7 +227,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
         const double2 g = G[p * ld + q];
         const double ag = cabs_(g);
         const double app = G[p * ld + p].x, aqq = G[q * ld + q].x;
-        const int rot = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)));
+        const int rot = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)) || ag <= floor_abs);
         s_p[i] = p;
         s_q[i] = q;
         s_flag[i] = rot;

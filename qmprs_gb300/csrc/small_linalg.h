@@ -34,6 +34,12 @@
 QM_HD void herm_eig_jacobi(double2* a, int n, double2* v, double* lam) {
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) v[i * n + j] = cd(i == j ? 1.0 : 0.0, 0.0);
+  // absolute floor: off-diagonals at most 1e-15 of the trace move no
+  // eigenvalue by more than that; without it the rounding-level null block
+  // of a rank-deficient matrix keeps rotating until the sweep limit
+  double tr = 0.0;
+  for (int i = 0; i < n; ++i) tr += fabs(a[i * n + i].x);
+  const double floor_abs = 1e-15 * tr;
   for (int sweep = 0; sweep < 60; ++sweep) {
     int rotated = 0;
     for (int p = 0; p < n - 1; ++p) {
@@ -41,7 +47,7 @@ QM_HD void herm_eig_jacobi(double2* a, int n, double2* v, double* lam) {
         double2 g = a[p * n + q];
         double ag = cabs_(g);
         double app = a[p * n + p].x, aqq = a[q * n + q].x;
-        if (ag == 0.0 || ag <= 1e-17 * sqrt(fabs(app * aqq))) continue;
+        if (ag == 0.0 || ag <= 1e-17 * sqrt(fabs(app * aqq)) || ag <= floor_abs) continue;
         rotated = 1;
         double zeta = (aqq - app) / (2.0 * ag);
         double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));

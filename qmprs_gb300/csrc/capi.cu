@@ -499,18 +499,11 @@ int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, do
       launch_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s);
     }
     launch_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s);
-    for (int j = 0; j < p->max_n; ++j) {
-      GateSel sel;
-      sel.mode = SEL_INVERSE;
-      sel.step = j;
-      sel.layer = l;
-      sel.adjoint = 1;
-      sel.gates = gates;
-      sel.arity = ar;
-      sel.nlayers = nullptr;
-      sel.active = p->active;
-      launch_apply_gate(p->bd, work, sel, s);
-    }
+    // inverse of the new layer: tile passes of two 4-qubit windows (up to
+    // six gates per read and write of the working state)
+    launch_layer_plan(p->bd, p->gd, ar, ORDER_LAYER_INV, l, p->active, s);
+    for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
+      launch_rebuild_pass(p->bd, p->gd, r, work, gates, ar, nullptr, p->active, s, ORDER_LAYER_INV, l);
     launch_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
     launch_count_active(p->B, p->active, p->num_active, s);
     int na = 0;
@@ -643,18 +636,11 @@ int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t
   if (!p || !vec || !gates || !arity) return QMPRS_ERR_INVALID;
   if (layer < 0 || layer >= p->max_layers) return set_err(p->h, QMPRS_ERR_INVALID, "layer index out of range");
   cudaStream_t s = (cudaStream_t)stream;
-  GateSel sel;
-  sel.mode = inverse ? SEL_INVERSE : SEL_LAYER_FWD;
-  sel.layer = layer;
-  sel.adjoint = inverse ? 1 : 0;
-  sel.gates = (const double2*)gates;
-  sel.arity = (const signed char*)arity;
-  sel.nlayers = nullptr;
-  sel.active = nullptr;
-  for (int j = 0; j < p->max_n; ++j) {
-    sel.step = j;
-    launch_apply_gate(p->bd, (float2*)vec, sel, s);
-  }
+  const int mode = inverse ? ORDER_LAYER_INV : ORDER_LAYER_FWD;
+  const signed char* ar = (const signed char*)arity;
+  launch_layer_plan(p->bd, p->gd, ar, mode, layer, nullptr, s);
+  for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
+    launch_rebuild_pass(p->bd, p->gd, r, (float2*)vec, (const double2*)gates, ar, nullptr, nullptr, s, mode, layer);
   CK(cudaGetLastError());
   return QMPRS_OK;
 }

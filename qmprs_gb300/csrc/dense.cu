@@ -76,11 +76,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_overlap(BatchDev bd, const fl
     tile_range(ipow2(n), bd.tile_idx[tile], nt, &lo, &hi);
     const float2* pa = a + bd.vec_off[b];
     const float2* pb = bv + bd.vec_off[b];
+    // exact fp32 products in compensated (double-float) sums, flushed to
+    // fp64 every TT_FLUSH elements: fp64-accurate at fp32 throughput
     double acc[2] = {0.0, 0.0};
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      double2 x = f2d(pa[i]), y = f2d(pb[i]);
-      acc[0] += x.x * y.x + x.y * y.y;
-      acc[1] += x.x * y.y - x.y * y.x;
+    int64_t i = lo + threadIdx.x;
+    while (i < hi) {
+      DF re = {0.f, 0.f}, im = {0.f, 0.f};
+      for (int f = 0; f < TT_FLUSH && i < hi; ++f, i += blockDim.x) {
+        const float2 x = pa[i], y = pb[i];
+        df_add_prod(re, x.x, y.x);   // conj(x) y
+        df_add_prod(re, x.y, y.y);
+        df_add_prod(im, x.x, y.y);
+        df_add_prod(im, -x.y, y.x);
+      }
+      acc[0] += (double)re.hi + (double)re.lo;
+      acc[1] += (double)im.hi + (double)im.lo;
     }
     block_sum<2>(acc);
     if (threadIdx.x == 0) partials[tile] = cd(acc[0], acc[1]);

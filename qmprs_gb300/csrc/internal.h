@@ -149,8 +149,14 @@ void launch_layer_fidelity(const BatchDev& bd, int layer, const float2* work, in
 // (d) sweep
 void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, const int* nlayers,
                        cudaStream_t s);
+// step orders of the group plan and the tile passes
+enum { ORDER_BWD = 0, ORDER_FWD = 1, ORDER_LAYER_INV = 2, ORDER_LAYER_FWD = 3 };
 void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
-                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s);
+                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s,
+                         int mode = ORDER_FWD, int layer = 0);
+void launch_layer_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, int mode, int layer,
+                       const int* active, cudaStream_t s);
+int layer_pass_bound(int max_n);
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
                       const double2* gates, const signed char* arity, const int* nlayers, const int* active,
                       cudaStream_t s);

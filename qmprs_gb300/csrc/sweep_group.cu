@@ -56,10 +56,22 @@ __device__ __forceinline__ bool fwd_step(const BatchDev& bd, const signed char* 
   return (*k == 1) || (*k == 2 && s <= n - 2);
 }
 
-__device__ __forceinline__ bool step_gate(bool forward, const BatchDev& bd, const signed char* arity, int L, int n,
-                                          int b, int j, int64_t* slot, int* q, int* k) {
-  return forward ? fwd_step(bd, arity, L, n, b, j, slot, q, k) : bwd_step(bd, arity, L, n, b, j, slot, q, k);
+// Gate at step j of a step order: backward sweep order, forward circuit
+// order, the inverse of one generated layer (sites n-1 .. 0, applied as
+// G^H) or one layer itself (sites 0 .. n-1).
+__device__ __forceinline__ bool step_gate(int mode, int layer, const BatchDev& bd, const signed char* arity, int L,
+                                          int n, int b, int j, int64_t* slot, int* q, int* k) {
+  if (mode == ORDER_BWD) return bwd_step(bd, arity, L, n, b, j, slot, q, k);
+  if (mode == ORDER_FWD) return fwd_step(bd, arity, L, n, b, j, slot, q, k);
+  if (j < 0 || j >= n) return false;
+  const int s = mode == ORDER_LAYER_INV ? n - 1 - j : j;
+  *slot = (int64_t)layer * n + s;
+  *q = s;
+  *k = arity[bd.gate_off[b] / 16 + *slot];
+  return (*k == 1) || (*k == 2 && s <= n - 2);
 }
+
+__device__ __forceinline__ int order_steps(int mode, int L, int n) { return mode <= ORDER_FWD ? L * n : n; }
 
 // Place the low bits of v, in order, at the set bits of mask (ascending).
 __device__ __forceinline__ int64_t deposit_bits(int64_t v, int64_t mask) {
@@ -82,18 +94,22 @@ __device__ __forceinline__ int swz(int li) { return li ^ (((li >> 4) ^ (li >> 8)
 
 // ---- group plan --------------------------------------------------------------
 
-// Groups of consecutive steps (backward sweep order, or the forward circuit
-// order when `forward`) whose qubits fit a window of min(GW, n) qubits.
-__global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers, int forward,
-                             GroupEnt* grp, int* ngroups) {
+// Groups of consecutive steps of a step order whose qubits fit a window of
+// min(GW, n) qubits.  States outside `active` (when given) get no groups.
+__global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity, const int* nlayers, int mode,
+                             int layer, const int* active, GroupEnt* grp, int* ngroups) {
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bd.B; b += gridDim.x * blockDim.x) {
-    const int n = bd.n[b], L = nlayers[b], total = L * n;
+    if (active && !active[b]) {
+      ngroups[b] = 0;
+      continue;
+    }
+    const int n = bd.n[b], L = mode <= ORDER_FWD ? nlayers[b] : 0, total = order_steps(mode, L, n);
     const int u = n < GW ? n : GW;
     int ng = 0, j = 0;
     while (j < total) {
       int64_t slot;
       int q, k;
-      if (!step_gate(forward, bd, arity, L, n, b, j, &slot, &q, &k)) {
+      if (!step_gate(mode, layer, bd, arity, L, n, b, j, &slot, &q, &k)) {
         atomicOr(bd.err, KERR_BAD_GATE);   // skipped, as the per-gate launches do
         ++j;
         continue;
@@ -101,7 +117,7 @@ __global__ void k_group_plan(BatchDev bd, GroupDev gd, const signed char* arity,
       int mask = (k == 2 ? 3 : 1) << q;
       const int j0 = j++;
       while (j < total && j - j0 < GMAXSTEPS) {
-        if (!step_gate(forward, bd, arity, L, n, b, j, &slot, &q, &k)) break;
+        if (!step_gate(mode, layer, bd, arity, L, n, b, j, &slot, &q, &k)) break;
         const int m2 = mask | ((k == 2 ? 3 : 1) << q);
         if (__popc(m2) > u) break;
         mask = m2;
@@ -500,7 +516,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
                                                                                  const double2* gates,
                                                                                  const signed char* arity,
                                                                                  const int* nlayers,
-                                                                                 const int* active) {
+                                                                                 const int* active, int mode,
+                                                                                 int layer) {
   extern __shared__ __align__(16) unsigned char dyn[];
   float2* xs = reinterpret_cast<float2*>(dyn);
   __shared__ RebuildShared sh;
@@ -511,7 +528,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
     const int ga = 2 * pass;
     if (ga >= ng) continue;
     const int n = bd.n[b];
-    const int L = nlayers[b];
+    const int L = mode <= ORDER_FWD ? nlayers[b] : 0;
     const int nw = ga + 1 < ng ? 2 : 1;
     GroupEnt ge[2];
     ge[0] = gd.rgrp[(int64_t)b * gd.gmax + ga];
@@ -523,7 +540,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
       const int w = threadIdx.x / GMAXSTEPS, st = threadIdx.x % GMAXSTEPS;
       int64_t slot;
       int q, k;
-      if (w < nw && st < ge[w].cnt && fwd_step(bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k)) {
+      if (w < nw && st < ge[w].cnt && step_gate(mode, layer, bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k)) {
         sh.pk[w][st] = k;
         sh.phi[w][st] = __popc(ge[w].qmask >> (q + 1));
         sh.plo[w][st] = k == 2 ? __popc(ge[w].qmask >> (q + 2)) : 0;
@@ -573,10 +590,13 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
       const int w = t / (GMAXSTEPS * 16), st = (t / 16) % GMAXSTEPS, e = t % 16;
       int64_t slot;
       int q, k;
-      if (w >= nw || st >= ge[w].cnt || !fwd_step(bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k)) continue;
+      if (w >= nw || st >= ge[w].cnt || !step_gate(mode, layer, bd, arity, L, n, b, ge[w].j0 + st, &slot, &q, &k))
+        continue;
       const int m = 1 << k;
       if (e >= m * m) continue;
-      const double2 v = gates[bd.gate_off[b] + slot * 16 + e];
+      const int r = e / m, c = e % m;
+      const double2 v = mode == ORDER_LAYER_INV ? cconj(gates[bd.gate_off[b] + slot * 16 + c * m + r])
+                                                : gates[bd.gate_off[b] + slot * 16 + e];
       sh.gm[w][st][e] = cf((float)v.x, (float)v.y);
     }
     __syncthreads();
@@ -751,18 +771,32 @@ void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char
                        cudaStream_t s) {
   const int blocks = (bd.B + 127) / 128;
   qm_note_launch();
-  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, 0, gd.grp, gd.ngroups);
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, ORDER_BWD, 0, nullptr, gd.grp, gd.ngroups);
   qm_note_launch();
-  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, 1, gd.rgrp, gd.nrgroups);
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nlayers, ORDER_FWD, 0, nullptr, gd.rgrp, gd.nrgroups);
+}
+
+void launch_layer_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, int mode, int layer,
+                       const int* active, cudaStream_t s) {
+  const int blocks = (bd.B + 127) / 128;
+  qm_note_launch();
+  k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nullptr, mode, layer, active, gd.rgrp, gd.nrgroups);
+}
+
+int layer_pass_bound(int max_n) {
+  // a group covers at least three new sites of the layer, except the last
+  const int groups = (max_n + 2) / 3 + 1;
+  return (groups + 1) / 2;
 }
 
 void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
-                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s) {
+                         const signed char* arity, const int* nlayers, const int* active, cudaStream_t s, int mode,
+                         int layer) {
   int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
   if (grid < 1) grid = 1;
   qm_note_launch();
   k_rebuild_pass<<<grid, PASS_THREADS, (size_t)sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
-                                                                          nlayers, active);
+                                                                          nlayers, active, mode, layer);
 }
 
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,

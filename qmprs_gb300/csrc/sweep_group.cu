@@ -699,10 +699,21 @@ __global__ void __launch_bounds__(POLAR_THREADS) k_group_polar(BatchDev bd, Grou
     const int n = bd.n[b], L = nlayers[b], D = 1 << ge.u;
     const int c0 = gd.state_chunk0[b], nc = gd.state_nchunks[b];
     __syncthreads();
+    // sum of the chunk partials in chunk order; eight chunks' loads are
+    // issued together so the L2 latency overlaps
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
       const int i = e / D, k = e % D;
+      const double2* src = gd.partials + (int64_t)c0 * GMM + i * GM + k;
       double2 s = czero();
-      for (int c = 0; c < nc; ++c) s = cadd(s, gd.partials[(int64_t)(c0 + c) * GMM + i * GM + k]);
+      int c = 0;
+      for (; c + 8 <= nc; c += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = src[(int64_t)(c + u) * GMM];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = cadd(s, v[u]);
+      }
+      for (; c < nc; ++c) s = cadd(s, src[(int64_t)c * GMM]);
       M[i * GM + k] = s;
     }
     __syncthreads();

@@ -47,6 +47,11 @@ struct qmprs_plan {
   int *d_chunk_state = nullptr, *d_chunk_idx = nullptr, *d_state_chunk0 = nullptr, *d_state_nchunks = nullptr,
       *d_ngroups = nullptr, *d_nrgroups = nullptr;
   GroupEnt *d_grp = nullptr, *d_rgrp = nullptr;
+  // stage (a) beyond bond 64: device-wide Jacobi scratch
+  int tt_w = TT_MAXW, tt_b = TT_MAXB;
+  WJRot* d_wj_rot = nullptr;
+  int *d_wj_count = nullptr, *d_wj_perm = nullptr;
+  double *d_wj_trace = nullptr, *d_wj_lam = nullptr;
   double2 *d_old_gates = nullptr, *d_gpartials = nullptr;
   GroupDev gd;
   // profiling of the sweep kernels (kernel classes: 0 environment stream,
@@ -185,6 +190,24 @@ void launch_count_active(int B, const int* active, int* num_active, cudaStream_t
   k_count_active<<<1, 256, 0, s>>>(B, active, num_active);
 }
 
+// Left-to-right contraction steps of the dense target for states whose bond
+// pair at this step exceeds the one-block kernel (bonds read on the host).
+void launch_wide_contract(qmprs_plan* p, int step, const double2* tensors, const std::vector<int>& hb,
+                          const float2* src, float2* dst_buf, float2* target, cudaStream_t s) {
+  const int stride = p->max_n + 1;
+  for (int b = 0; b < p->B; ++b) {
+    const int n = p->n[b], c = step + 1;
+    if (c > n - 1) continue;
+    const int rc = hb[(size_t)b * stride + c], rn = hb[(size_t)b * stride + c + 1];
+    if (rc < 1 || rn < 1 || rc > p->tt_b || rn > p->tt_b) continue;
+    if (rc <= TT_MAXB && rn <= TT_MAXB) continue;
+    const int ce = chi_eff_host(p->max_bond, n);
+    const double2* a = tensors + p->tensor_off[b] + (int64_t)c * 2 * ce * ce;
+    float2* o = (c == n - 1 ? target : dst_buf) + p->vec_off[b];
+    launch_cgemm(src + p->vec_off[b], rc, a, 2 * rn, o, 2 * rn, ipow2(c), 2 * rn, rc, s);
+  }
+}
+
 extern "C" {
 
 int qmprs_version(void) { return 100; }
@@ -236,7 +259,8 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->bonds,    p->active,       p->nlayers,    p->num_active,    p->nuc,
                   p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
                   p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials,
-                  p->d_rgrp,   p->d_nrgroups};
+                  p->d_rgrp,   p->d_nrgroups,   p->d_wj_rot,  p->d_wj_count,  p->d_wj_perm,
+                  p->d_wj_trace, p->d_wj_lam};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -290,6 +314,8 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
     }
   }
   p->ntiles = (int)tile_state.size();
+  for (int b = 0; b < num_states; ++b) p->tt_b = std::max(p->tt_b, chi_eff_host(max_bond, p->n[b]));
+  p->tt_w = std::max(TT_MAXW, 2 * p->tt_b);
   // grouped sweep: tiles of 2^min(n, GT) amplitudes, GCHUNK tiles per chunk
   std::vector<int> chunk_state, chunk_idx, state_chunk0(num_states), state_nchunks(num_states);
   for (int b = 0; b < num_states; ++b) {
@@ -398,6 +424,8 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   bd.state_ntiles = p->d_state_ntiles;
   bd.ticket = p->d_ticket;
   bd.err = p->d_err;
+  bd.tt_w = p->tt_w;
+  bd.tt_b = p->tt_b;
   *out = p;
   return QMPRS_OK;
 }
@@ -429,31 +457,84 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
   float2* target = (float2*)target_;
   double2* tensors = (double2*)tensors_;
   for (int b = 0; b < p->B; ++b)
-    if (chi_eff_host(max_bond, p->n[b]) > TT_MAXB)
+    if (chi_eff_host(max_bond, p->n[b]) > TT_WIDE_MAXB)
       return set_err(p->h, QMPRS_ERR_UNSUPPORTED,
-                     "statevector -> MPS supports bond dimensions up to 64 (min(bond_dimension, 2^(n/2)) > 64)");
-  const int WW = TT_MAXW * TT_MAXW;
+                     "statevector -> MPS supports bond dimensions up to 1024 (min(bond_dimension, 2^(n/2)) > 1024)");
+  const int64_t WW = (int64_t)p->tt_w * p->tt_w;
+  const bool wide = p->tt_b > TT_MAXB;
   if (!p->tt_partials) {
     CK(dalloc(&p->tt_partials, (int64_t)p->B * TT_SPLIT * WW));
     CK(dalloc(&p->gram, (int64_t)p->B * WW));
     CK(dalloc(&p->vsel2, (int64_t)p->B * WW));
     CK(dalloc(&p->vwork, (int64_t)p->B * WW));
+    if (wide) {
+      CK(cudaMalloc(reinterpret_cast<void**>(&p->d_wj_rot), wj_rot_bytes(p->tt_w)));
+      CK(dalloc(&p->d_wj_count, 1));
+      CK(dalloc(&p->d_wj_trace, 1));
+      CK(dalloc(&p->d_wj_perm, p->tt_w));
+      CK(dalloc(&p->d_wj_lam, p->tt_w));
+    }
   }
   CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
   const int64_t nb = (int64_t)p->B * (p->max_n + 1);
   CK(cudaMemcpyAsync(bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
   launch_overlap(p->bd, sv, sv, p->partials, p->sq, s);
   float2* buf[2] = {p->S0, p->S1};
+  const int stride = p->max_n + 1;
+  std::vector<int> hb(wide ? (size_t)p->B * stride : 0);
+  auto read_bonds = [&]() -> int {
+    CK(cudaMemcpyAsync(hb.data(), bonds, sizeof(int) * hb.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return QMPRS_OK;
+  };
   for (int j = 0; j + 2 <= p->max_n; ++j) {
     const float2* src = j == 0 ? sv : buf[(j - 1) & 1];
     launch_tt_gram(p->bd, j, sv, src, bonds, p->tt_partials, p->gram, s);
     launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond, s);
     launch_tt_project(p->bd, j, sv, src, buf[j & 1], bonds, p->vsel2, s);
+    // Grams wider than 128 and projections to more than 64 columns: the
+    // device-wide path, state by state (possible only after 6 cuts)
+    if (wide && j >= 6) {
+      int rc = read_bonds();
+      if (rc != QMPRS_OK) return rc;
+      bool any = false;
+      for (int b = 0; b < p->B; ++b) {
+        const int c = p->n[b] - 1 - j;
+        if (c < 1) continue;
+        const int r = hb[(size_t)b * stride + c + 1];
+        if (r < 1 || r > p->tt_b || 2 * r <= TT_MAXW) continue;
+        const int e = tt_wide_eig(p->bd, b, c, 2 * r, p->gram, p->vwork, p->d_wj_rot, p->d_wj_count,
+                                  p->d_wj_trace, p->d_wj_perm, p->d_wj_lam, bonds, p->vsel2, tensors,
+                                  p->max_bond, max_bond, cutoff, s);
+        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) device-wide Jacobi");
+        any = true;
+      }
+      if (any) {
+        rc = read_bonds();
+        if (rc != QMPRS_OK) return rc;
+      }
+      for (int b = 0; b < p->B; ++b) {
+        const int c = p->n[b] - 1 - j;
+        if (c < 1) continue;
+        const int r = hb[(size_t)b * stride + c + 1], keep = hb[(size_t)b * stride + c];
+        if (r < 1 || keep < 1 || r > p->tt_b || keep > p->tt_b) continue;
+        if (2 * r <= TT_MAXW && keep <= TT_MAXB) continue;
+        const int w = 2 * r;
+        const float2* m = src + p->vec_off[b];
+        launch_cgemm(m, w, p->vsel2 + (int64_t)b * WW, p->tt_b, buf[j & 1] + p->vec_off[b], keep, ipow2(c), keep, w,
+                     s);
+      }
+    }
   }
   launch_tt_site0(p->bd, buf[0], buf[1], bonds, tensors, p->max_bond, p->sq, s);
+  if (wide) {
+    const int rc = read_bonds();
+    if (rc != QMPRS_OK) return rc;
+  }
   for (int j = 0; j + 2 <= p->max_n; ++j) {
     const float2* src = j == 0 ? buf[0] : buf[(j - 1) & 1];
     launch_mps_contract(p->bd, j, tensors, bonds, p->max_bond, src, buf[j & 1], target, s);
+    if (wide) launch_wide_contract(p, j, tensors, hb, src, buf[j & 1], target, s);
   }
   return check_kernel_errors(p, s);
 }
@@ -462,9 +543,16 @@ int qmprs_mps_to_statevector(qmprs_plan_t p, const void* tensors, const int* bon
   if (!p || !tensors || !bonds || !out) return QMPRS_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   float2* buf[2] = {p->S0, p->S1};
+  const bool wide = p->tt_b > TT_MAXB;
+  std::vector<int> hb(wide ? (size_t)p->B * (p->max_n + 1) : 0);
+  if (wide) {
+    CK(cudaMemcpyAsync(hb.data(), bonds, sizeof(int) * hb.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
   for (int j = 0; j + 2 <= p->max_n; ++j) {
     const float2* src = j == 0 ? buf[0] : buf[(j - 1) & 1];
     launch_mps_contract(p->bd, j, (const double2*)tensors, bonds, p->max_bond, src, buf[j & 1], (float2*)out, s);
+    if (wide) launch_wide_contract(p, j, (const double2*)tensors, hb, src, buf[j & 1], (float2*)out, s);
   }
   CK(cudaGetLastError());
   return QMPRS_OK;

@@ -35,8 +35,9 @@
 #define WARPS_PER_BLOCK 8   // BLOCK_THREADS / 32; per-warp partials per tile
 #define BLOCK_THREADS 256
 #define MAX_QUBITS 30
-#define TT_MAXW 128   // widest Gram of stage (a): 2 * bond
-#define TT_MAXB 64    // largest MPS bond of stage (a)
+#define TT_MAXW 128   // widest Gram of stage (a)'s one-block kernels: 2 * bond
+#define TT_MAXB 64    // largest bond of stage (a)'s one-block kernels (wider: ttsvd_wide.cu)
+#define TT_WIDE_MAXB 1024   // largest bond of stage (a) overall
 
 enum {
   QM_OK = 0,
@@ -70,6 +71,8 @@ struct BatchDev {
   const int* state_ntiles; // [B]
   int* ticket;             // [B] last-tile tickets (kept at zero between launches)
   int* err;                // [1] error flag bits
+  int tt_w;                // stage (a): Gram stride (>= TT_MAXW, 2 x the largest bond)
+  int tt_b;                // stage (a): largest bond / selected-column stride (>= TT_MAXB)
 };
 
 // Gate selection modes for the per-step gate launches.
@@ -175,6 +178,13 @@ void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const flo
                        const int* bonds, const double2* vsel, cudaStream_t s);
 void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1, const int* bonds,
                      double2* tensors, int chi, const double2* in_sq, cudaStream_t s);
+struct WJRot;
+int tt_wide_eig(const BatchDev& bd, int b, int c, int w, double2* gram, double2* vwork, WJRot* rot, int* d_count,
+                double* d_trace, int* perm, double* lam, int* bonds, double2* vsel, double2* tensors, int chi,
+                int max_bond, double cutoff, cudaStream_t s);
+void launch_cgemm(const float2* A, int64_t lda, const double2* B, int64_t ldb, float2* C, int64_t ldc, int64_t M,
+                  int N, int K, cudaStream_t s);
+size_t wj_rot_bytes(int w);
 void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,
                          const float2* src, float2* dst_buf, float2* target, cudaStream_t s);
 

@@ -30,7 +30,7 @@ __host__ __device__ inline int chi_eff(int chi, int n) {
   return chi < cap ? chi : cap;
 }
 
-__device__ __forceinline__ bool bond_ok(int r) { return r >= 1 && r <= TT_MAXB; }
+__device__ __forceinline__ bool bond_ok(int r, int lim) { return r >= 1 && r <= lim; }
 
 #define TT_EPB 8   // entries per thread: a 2 x 4 block (a in {2i, 2i+1}, cc in {4j .. 4j+3})
 
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
                                                            const float2* src, const int* bonds,
                                                            double2* partials, double2* gram) {
   __shared__ double2 red[BLOCK_THREADS * TT_EPB];   // 32 KB
-  const int WW = TT_MAXW * TT_MAXW;
+  const int64_t WW = (int64_t)bd.tt_w * bd.tt_w;
   for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
     const int b = bd.tile_state[tile];
     const int n = bd.n[b];
@@ -75,20 +75,26 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
     const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
     const int r = bond[c + 1];
     const int idx = bd.tile_idx[tile];
-    if (!bond_ok(r)) {
-      if (r > TT_MAXB && idx == 0 && threadIdx.x == 0) atomicOr(bd.err, KERR_EIG_WIDTH);
+    if (!bond_ok(r, bd.tt_b)) {
+      if (r > bd.tt_b && idx == 0 && threadIdx.x == 0) atomicOr(bd.err, KERR_EIG_WIDTH);
       continue;
     }
     const int w = 2 * r;
     const int nt = bd.state_ntiles[b];
     const int nsplit = nt < TT_SPLIT ? nt : TT_SPLIT;
-    if (idx >= nsplit) continue;
     const float2* m = (step == 0 ? sv : src) + bd.vec_off[b];
-    int64_t lo, hi;
-    tile_range(ipow2(c), idx, nsplit, &lo, &hi);
-    double2* part = partials + ((int64_t)b * TT_SPLIT + idx) * WW;
     const int nb = gram_nblocks(w);
-    for (int e0 = 0; e0 < nb; e0 += BLOCK_THREADS) {
+    // work units: (row split, chunk of BLOCK_THREADS entry blocks), taken by
+    // the state's tiles in turn, so wide Grams spread over many blocks
+    const int nech = (nb + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    const int units = nsplit * nech;
+    for (int unit = idx; unit < units; unit += nt) {
+    const int split = unit % nsplit;
+    int64_t lo, hi;
+    tile_range(ipow2(c), split, nsplit, &lo, &hi);
+    double2* part = partials + ((int64_t)b * TT_SPLIT + split) * WW;
+    {
+      const int e0 = (unit / nsplit) * BLOCK_THREADS;
       const int nbp = nb - e0 < BLOCK_THREADS ? nb - e0 : BLOCK_THREADS;
       const int nsub = BLOCK_THREADS / nbp;
       const int eb = threadIdx.x % nbp, sub = threadIdx.x / nbp;
@@ -142,23 +148,24 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
         int gi, gj;
         gram_block(e0 + ebo, w, &gi, &gj);
         const int a = 2 * gi + k / 4, cc = 4 * gj + k % 4;
-        if (a <= cc && cc < w) part[a * w + cc] = sacc;
+        if (a <= cc && cc < w) part[(int64_t)a * w + cc] = sacc;
       }
     }
     __syncthreads();
-    if (last_tile_ticket(bd.ticket, b, nsplit)) {
+    if (last_tile_ticket(bd.ticket, b, units)) {
       for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
         const int a = e / w, cc = e % w;
         if (a > cc) continue;
         double2 s = czero();
         for (int t = 0; t < nsplit; ++t) s = cadd(s, ld_cg(&partials[((int64_t)b * TT_SPLIT + t) * WW + a * w + cc]));
-        gram[(int64_t)b * WW + a * w + cc] = s;
-        if (a != cc) gram[(int64_t)b * WW + cc * w + a] = cconj(s);
-        else gram[(int64_t)b * WW + a * w + a] = cd(s.x, 0.0);
+        gram[(int64_t)b * WW + (int64_t)a * w + cc] = s;
+        if (a != cc) gram[(int64_t)b * WW + (int64_t)cc * w + a] = cconj(s);
+        else gram[(int64_t)b * WW + (int64_t)a * w + a] = cd(s.x, 0.0);
       }
       __syncthreads();
       if (threadIdx.x == 0) bd.ticket[b] = 0;
     }
+    }   // units
   }
 }
 
@@ -178,7 +185,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   __shared__ double s_lam[TT_MAXW];
   __shared__ int s_perm[TT_MAXW];
   __shared__ int s_keep;
-  const int WW = TT_MAXW * TT_MAXW;
+  const int64_t WW = (int64_t)bd.tt_w * bd.tt_w;
   const int b = blockIdx.x;
   if (b >= bd.B) return;
   const int n = bd.n[b];
@@ -186,11 +193,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   if (c < 1) return;
   int* bond = bonds + (int64_t)b * (bd.max_n + 1);
   const int r = bond[c + 1];
-  if (!bond_ok(r)) {
+  if (!bond_ok(r, bd.tt_b)) {
     if (threadIdx.x == 0) bond[c] = -1;   // poison: every later step skips this state
     return;
   }
   const int w = 2 * r;
+  if (w > TT_MAXW) return;   // diagonalised by the device-wide solver (ttsvd_wide.cu)
   extern __shared__ double2 eig_sm[];
   double2* Gg = gram + (int64_t)b * WW;
   double2* Vg = vwork + (int64_t)b * WW;
@@ -292,7 +300,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
       s_perm[j + 1] = kk;
     }
     int keep = rank_by_cutoff(s_lam, w, cutoff, max_bond);
-    if (keep > TT_MAXB) keep = TT_MAXB;
+    if (keep > bd.tt_b) keep = bd.tt_b;
     if (c < 30 && keep > (1 << c)) keep = 1 << c;   // M has 2^c rows: rank <= 2^c
     s_keep = keep;
     bond[c] = keep;
@@ -304,7 +312,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   double2* vs = vsel + (int64_t)b * WW;
   for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
     const int a = e / keep, col = e % keep;
-    vs[a * TT_MAXB + col] = V[a * ld + s_perm[col]];
+    vs[(int64_t)a * bd.tt_b + col] = V[a * ld + s_perm[col]];
   }
   const int ce = chi_eff(chi, n);
   double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
@@ -321,7 +329,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_project(BatchDev bd, int s
   extern __shared__ float2 sh[];
   float2* vs = sh;
   float2* xs = sh + TT_MAXW * TT_MAXB;
-  const int WW = TT_MAXW * TT_MAXW;
+  const int64_t WW = (int64_t)bd.tt_w * bd.tt_w;
   for (int tile = blockIdx.x; tile < bd.ntiles; tile += gridDim.x) {
     const int b = bd.tile_state[tile];
     const int n = bd.n[b];
@@ -330,11 +338,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_project(BatchDev bd, int s
     const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
     const int r = bond[c + 1];
     const int keep = bond[c];
-    if (!bond_ok(r) || !bond_ok(keep)) continue;
+    if (!bond_ok(r, bd.tt_b) || !bond_ok(keep, bd.tt_b)) continue;
     const int w = 2 * r;
+    if (w > TT_MAXW || keep > TT_MAXB) continue;   // projected by k_cgemm
     __syncthreads();
     for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
-      const double2 v = vsel[(int64_t)b * WW + (e / keep) * TT_MAXB + (e % keep)];
+      const double2 v = vsel[(int64_t)b * WW + (int64_t)(e / keep) * bd.tt_b + (e % keep)];
       vs[e] = cf((float)v.x, (float)v.y);
     }
     const float2* m = (step == 0 ? sv : src) + bd.vec_off[b];
@@ -363,7 +372,7 @@ __global__ void k_tt_site0(BatchDev bd, const float2* rem0, const float2* rem1, 
     const int n = bd.n[b];
     const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
     const int r1 = bond[1];
-    if (!bond_ok(r1)) continue;
+    if (!bond_ok(r1, bd.tt_b)) continue;
     const float2* rem = (((n - 2) & 1) ? rem1 : rem0) + bd.vec_off[b];
     double nrm = 0.0;
     for (int i = 0; i < 2 * r1; ++i) nrm += cnorm2(f2d(rem[i]));
@@ -388,7 +397,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_mps_contract(BatchDev bd, int
     if (c > n - 1) continue;
     const int* bond = bonds + (int64_t)b * (bd.max_n + 1);
     const int rc = bond[c], rn = bond[c + 1];
-    if (!bond_ok(rc) || !bond_ok(rn)) continue;
+    if (!bond_ok(rc, bd.tt_b) || !bond_ok(rn, bd.tt_b)) continue;
+    if (rc > TT_MAXB || rn > TT_MAXB) continue;   // contracted by k_cgemm
     const int ce = chi_eff(chi, n);
     const double2* a = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
     __syncthreads();

@@ -193,8 +193,8 @@ class MPS:
         n = len(tensors)
         bonds = [1] + [int(t.shape[2]) for t in tensors[:-1]] + [1]
         chi = max(bonds)
-        if chi > 64:
-            raise ValueError("MPS bonds above 64 are not supported on the GPU path")
+        if chi > 1024:
+            raise ValueError("MPS bonds above 1024 are not supported on the GPU path")
         eng = _engine.engine()
         p = eng.plan([n], 1, chi)
         ce = p.chi_eff(0)

@@ -58,6 +58,25 @@ def test_sv_to_mps(eng, ns, chi):
             assert np.allclose(got[s], ref[s], atol=GATE_TOL), (b, s)
 
 
+@pytest.mark.parametrize("n,chi", [(16, 128), (18, 256), (16, 100)])
+def test_sv_to_mps_wide_bonds(eng, n, chi):
+    """Bonds above 64 (Grams wider than 128: the device-wide Jacobi and the
+    tiled projection and contraction): bonds equal to the oracle's, site
+    tensors to GATE_TOL, and the dense truncated target."""
+    sv = S.uniform_complex(n, 5 + n)
+    res = eng.encode([sv], chi, num_layers=1, num_sweeps=0, keep_tensors=True)
+    sv64 = sv.astype(np.complex64).astype(np.complex128)
+    ref = D.tt_svd_right(sv64 / np.linalg.norm(sv64), n, chi)
+    got = res.mps_tensors(0)
+    assert [t.shape for t in got] == [t.shape for t in ref]
+    assert max(t.shape[2] for t in ref[:-1]) > 64
+    for s_, (g, r) in enumerate(zip(got, ref)):
+        assert np.allclose(g, r, atol=GATE_TOL), s_
+    t = D.mps_to_dense(ref)
+    tg = D.mps_to_dense(got)
+    assert abs(abs(np.vdot(t, tg)) / (np.linalg.norm(t) * np.linalg.norm(tg)) - 1) < 1e-6
+
+
 def test_untruncated_reconstruction(eng):
     from qmprs_gb300 import engine as E
     import torch

@@ -174,6 +174,37 @@ __device__ __forceinline__ int deposit32(int v, int mask) {
   return r;
 }
 
+// Tile offset of rest index r.  Rest index bits 0 and 1 go to rest tile
+// bits whose bank residues (bit position mod 4: the swizzle folds tile bits
+// 4-7 and 8-11 onto 0-3) differ from each other and from those of the
+// window's two lowest bits, so that the 16 tensor-core fragment loads of a
+// half-warp (window entries 0-3 times rests 0-3) hit 16 distinct bank
+// pairs; the other rest bits follow in ascending order.  The reduction over
+// rests does not depend on their order.
+__device__ __forceinline__ int rest_offset(int r, int wmask, int rmask) {
+  int cov = 0, m = wmask;
+  for (int i = 0; i < 2 && m; ++i) {
+    cov |= 1 << ((__ffs(m) - 1) & 3);
+    m &= m - 1;
+  }
+  int lead[2], left = rmask;
+  for (int i = 0; i < 2; ++i) {
+    int pick = 0;
+    for (int mm = left; mm; mm &= mm - 1) {
+      const int bit = __ffs(mm) - 1;
+      if (!((cov >> (bit & 3)) & 1)) {
+        pick = 1 << bit;
+        break;
+      }
+    }
+    if (!pick) pick = left & (-left);
+    lead[i] = pick;   // zero when the rest has fewer bits
+    if (pick) cov |= 1 << ((__ffs(pick) - 1) & 3);
+    left &= ~pick;
+  }
+  return ((r & 1) ? lead[0] : 0) | ((r & 2) ? lead[1] : 0) | deposit32(r >> 2, left);
+}
+
 // Previous group's peels on x and new gates on z, over the previous
 // window: a thread owns the 2^U amplitudes of one window position and
 // applies the group's gates in registers.
@@ -256,6 +287,105 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
   __syncthreads();
 }
 
+// ---- cross matrix on the tensor cores (4-qubit windows) -----------------------
+//
+// M = conj(Z) X^T with Z, X the 16 x rest matrices of the tile, as real
+// m16n8k8 TF32 products (rows: window entry of z, columns: window entry of
+// x, reduction: rests):
+//   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T.
+// Each fp32 operand v is split v = hi + lo with hi = tf32(v) and
+// lo = tf32(v - hi) (v - hi is exact in fp32); a product is taken as
+// lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32 scheme), which leaves a
+// relative error of about 2^-21 per product.  A warp owns k-steps of
+// 8 rests; its fragments come straight from the swizzled tile (no staging):
+// lane (g, t) reads rows/columns g and g + 8 at rests 8 s + t and 8 s + t + 4.
+// Accumulators: acc[nt][0] = Re, acc[nt][1] = Zr Xi^T, acc[nt][2] = Zi Xr^T
+// for the column tiles nt = 0 (entries 0..7) and 1 (8..15).
+__device__ __forceinline__ void tf32_split(float v, unsigned& hi, unsigned& lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(hi) : "f"(v));
+  const float r = v - __uint_as_float(hi);
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(lo) : "f"(r));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// c += a b, the small products first
+__device__ __forceinline__ void mma3(float (&c)[4], const unsigned (&ah)[4], const unsigned (&al)[4],
+                                     const unsigned (&bh)[2], const unsigned (&bl)[2]) {
+  mma_tf32(c, al, bh[0], bh[1]);
+  mma_tf32(c, ah, bl[0], bl[1]);
+  mma_tf32(c, ah, bh[0], bh[1]);
+}
+
+// Needs 2^(T - 4) >= 8 rests.
+__device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2* xs, const float2* zs,
+                                              float (&acc)[2][3][4]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const int w0 = sh.wl[gq], w1 = sh.wl[gq + 8];
+  const int nks = 1 << (sh.T - 7);
+  for (int ks = warp; ks < nks; ks += nwarps) {
+    const int r0 = sh.rl[ks * 8 + tq], r1 = sh.rl[ks * 8 + tq + 4];
+    // A = Z: a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4)
+    const float2 z0 = zs[w0 ^ r0], z1 = zs[w1 ^ r0], z2 = zs[w0 ^ r1], z3 = zs[w1 ^ r1];
+    // B = X^T, column tile nt: b0 (rest t, entry 8 nt + g), b1 (rest t + 4, same entry)
+    const float2 x0 = xs[w0 ^ r0], x1 = xs[w0 ^ r1], x2 = xs[w1 ^ r0], x3 = xs[w1 ^ r1];
+    unsigned zrh[4], zrl[4], zih[4], zil[4];
+    tf32_split(z0.x, zrh[0], zrl[0]);
+    tf32_split(z1.x, zrh[1], zrl[1]);
+    tf32_split(z2.x, zrh[2], zrl[2]);
+    tf32_split(z3.x, zrh[3], zrl[3]);
+    tf32_split(z0.y, zih[0], zil[0]);
+    tf32_split(z1.y, zih[1], zil[1]);
+    tf32_split(z2.y, zih[2], zil[2]);
+    tf32_split(z3.y, zih[3], zil[3]);
+    unsigned xrh[2][2], xrl[2][2], xih[2][2], xil[2][2];
+    tf32_split(x0.x, xrh[0][0], xrl[0][0]);
+    tf32_split(x1.x, xrh[0][1], xrl[0][1]);
+    tf32_split(x2.x, xrh[1][0], xrl[1][0]);
+    tf32_split(x3.x, xrh[1][1], xrl[1][1]);
+    tf32_split(x0.y, xih[0][0], xil[0][0]);
+    tf32_split(x1.y, xih[0][1], xil[0][1]);
+    tf32_split(x2.y, xih[1][0], xil[1][0]);
+    tf32_split(x3.y, xih[1][1], xil[1][1]);
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      mma3(acc[nt][0], zrh, zrl, xrh[nt], xrl[nt]);
+      mma3(acc[nt][0], zih, zil, xih[nt], xil[nt]);
+      mma3(acc[nt][1], zrh, zrl, xih[nt], xil[nt]);
+      mma3(acc[nt][2], zih, zil, xrh[nt], xrl[nt]);
+    }
+  }
+}
+
+// Sum the warps' M (fixed order) into the chunk's partial.  `red` aliases
+// the tile buffers (needs nwarps * 256 double2).
+__device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][3][4], double2* red, double2* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  __syncthreads();   // tile buffers free
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int i = gq + (e >> 1) * 8, k = nt * 8 + 2 * tq + (e & 1);
+      red[warp * GMM + i * GM + k] =
+          cd((double)acc[nt][0][e], (double)acc[nt][1][e] - (double)acc[nt][2][e]);
+    }
+  __syncthreads();
+  for (int ent = threadIdx.x; ent < GMM; ent += blockDim.x) {
+    double2 s = czero();
+    for (int w = 0; w < nwarps; ++w) s = cadd(s, red[w * GMM + ent]);
+    out[ent] = s;
+  }
+  __syncthreads();
+}
+
 // Tile loads: 8-byte cp.async copies straight into swizzled shared memory,
 // one commit group per tile, so the next tile streams in while the current
 // one is processed.
@@ -320,19 +450,24 @@ __device__ __forceinline__ void pass_store(const PassShared& sh, float2* xg, flo
 // read as a counter
 __device__ __forceinline__ int64_t next_in_mask(int64_t x, int64_t mask) { return ((x | ~mask) + 1) & mask; }
 
-template <int U>
+// TC: the cross matrix on the tensor cores (U = 4, T >= 7).
+template <int U, bool TC>
 __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& gd, const PassShared& sh, float2* xs,
                                            float2* zs, int g, int b, int chunk, float2* psi, const float2* z_in,
                                            float2* z_out) {
+  static_assert(!TC || U == 4, "tensor-core cross needs 16-entry windows");
   const int n = bd.n[b];
   const int64_t ntiles = (int64_t)1 << (n - sh.T);
   const int64_t rest_mask = (((int64_t)1 << n) - 1) & ~(int64_t)sh.pos_mask;
   float2* xv = psi + bd.vec_off[b];
   const float2* zv_in = z_in + bd.vec_off[b];
   float2* zv_out = z_out + bd.vec_off[b];
-  float2 acc[16];
+  float2 acc[TC ? 1 : 16];
+  float tacc[2][3][4];
 #pragma unroll
-  for (int e = 0; e < 16; ++e) acc[e] = cf(0.f, 0.f);
+  for (int e = 0; e < (TC ? 1 : 16); ++e) acc[e] = cf(0.f, 0.f);
+#pragma unroll
+  for (int e = 0; e < 24; ++e) (&tacc[0][0][0])[e] = 0.f;
   const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
   const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
   int64_t base = deposit_bits(t0, rest_mask);
@@ -346,11 +481,13 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
       __syncthreads();
       pass_store(sh, xv + base, zv_out + base, xs, zs);
     }
-    pass_cross<U>(sh, xs, zs, acc);
+    if constexpr (TC) pass_cross_tc(sh, xs, zs, tacc);
+    else pass_cross<U>(sh, xs, zs, acc);
     __syncthreads();
     base = next_in_mask(base, rest_mask);
   }
-  pass_flush<U>(acc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
+  if constexpr (TC) pass_flush_tc(tacc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
+  else pass_flush<U>(acc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
 }
 
 __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass(BatchDev bd, GroupDev gd, int g, float2* psi,
@@ -423,7 +560,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       sh.wlp[a] = swz(deposit32(a, sh.wml_p));
     }
     for (int r = threadIdx.x; r < (1 << (T - U)); r += blockDim.x) {
-      sh.rl[r] = swz(deposit32(r, full & ~sh.wml_c));
+      sh.rl[r] = swz(rest_offset(r, sh.wml_c, full & ~sh.wml_c));
       sh.plp[r] = swz(deposit32(r, full & ~sh.wml_p));
     }
     if (g > 0) {
@@ -445,9 +582,10 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       }
     }
     __syncthreads();
-    if (U == 4) pass_chunk<4>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
-    else if (U == 3) pass_chunk<3>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
-    else pass_chunk<2>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    if (U == 4 && T >= 7) pass_chunk<4, true>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    else if (U == 4) pass_chunk<4, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    else if (U == 3) pass_chunk<3, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    else pass_chunk<2, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
   }
 }
 

@@ -151,6 +151,7 @@ struct PassShared {
   int plp[1 << (GT - GW)];  // rest index -> swizzled tile offset (previous window)
   int d0[64], d1[64];       // global offset of tile index li: d0[li & 63] | d1[li >> 6]
   float2 gm[2][GMAXSTEPS][16];   // [peel | new][step]: the applied matrix, row-major complex
+  uint4 gf[2][2][4][32];    // [side][k-step][Gr hi, Gr lo, Gi hi, Gi lo][lane]: tensor-core A fragments
 };
 
 // Dynamic shared memory: the tile of x and of z (float2 each).  Four blocks
@@ -181,28 +182,55 @@ __device__ __forceinline__ int deposit32(int v, int mask) {
 // half-warp (window entries 0-3 times rests 0-3) hit 16 distinct bank
 // pairs; the other rest bits follow in ascending order.  The reduction over
 // rests does not depend on their order.
-__device__ __forceinline__ int rest_offset(int r, int wmask, int rmask) {
-  int cov = 0, m = wmask;
-  for (int i = 0; i < 2 && m; ++i) {
-    cov |= 1 << ((__ffs(m) - 1) & 3);
-    m &= m - 1;
+// bank residue (one-hot) of a single-bit mask; 0 for no bit
+__device__ __forceinline__ int bank_res(int bit) { return bit ? 1 << ((__ffs(bit) - 1) & 3) : 0; }
+
+// lowest bit of `left` whose residue is not in `avoid`, else 0
+__device__ __forceinline__ int pick_res(int left, int avoid) {
+  for (int m = left; m; m &= m - 1) {
+    const int bit = __ffs(m) - 1;
+    if (!((avoid >> (bit & 3)) & 1)) return 1 << bit;
   }
-  int lead[2], left = rmask;
+  return 0;
+}
+
+// residues of the two lowest bits of a window mask
+__device__ __forceinline__ int low2_res(int wmask) {
+  const int b0 = wmask & (-wmask), rest = wmask & ~b0;
+  return bank_res(b0) | bank_res(rest & (-rest));
+}
+
+__device__ __forceinline__ int rest_offset(int r, int wmask, int rmask) {
+  int cov = low2_res(wmask), left = rmask, lead[2];
   for (int i = 0; i < 2; ++i) {
-    int pick = 0;
-    for (int mm = left; mm; mm &= mm - 1) {
-      const int bit = __ffs(mm) - 1;
-      if (!((cov >> (bit & 3)) & 1)) {
-        pick = 1 << bit;
-        break;
-      }
-    }
+    int pick = pick_res(left, cov);
     if (!pick) pick = left & (-left);
     lead[i] = pick;   // zero when the rest has fewer bits
-    if (pick) cov |= 1 << ((__ffs(pick) - 1) & 3);
+    cov |= bank_res(pick);
     left &= ~pick;
   }
   return ((r & 1) ? lead[0] : 0) | ((r & 2) ? lead[1] : 0) | deposit32(r >> 2, left);
+}
+
+// Tile offset of window position p for the tensor-core gate application.
+// Its loads put window bits 0-1 and position bits 0-1 on a half-warp, its
+// stores window bits 0-1 and position bits 1-2, so position bit 1 takes a
+// residue outside the window's, bit 0 a fourth one and bit 2 the residue of
+// bit 0 where the tile has one.
+__device__ __forceinline__ int apply_pos_offset(int p, int wmask, int rmask) {
+  const int cov = low2_res(wmask);
+  int left = rmask;
+  int p1 = pick_res(left, cov);
+  if (!p1) p1 = left & (-left);
+  left &= ~p1;
+  int p0 = pick_res(left, cov | bank_res(p1));
+  if (!p0) p0 = left & (-left);
+  left &= ~p0;
+  int p2 = pick_res(left, 15 & ~bank_res(p0));
+  if (!p2 || !p0) p2 = pick_res(left, cov | bank_res(p1));
+  if (!p2) p2 = left & (-left);
+  left &= ~p2;
+  return ((p & 1) ? p0 : 0) | ((p & 2) ? p1 : 0) | ((p & 4) ? p2 : 0) | deposit32(p >> 3, left);
 }
 
 // Previous group's peels on x and new gates on z, over the previous
@@ -293,18 +321,20 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
 // m16n8k8 TF32 products (rows: window entry of z, columns: window entry of
 // x, reduction: rests):
 //   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T.
-// Each fp32 operand v is split v = hi + lo with hi = tf32(v) and
-// lo = tf32(v - hi) (v - hi is exact in fp32); a product is taken as
-// lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32 scheme), which leaves a
-// relative error of about 2^-21 per product.  A warp owns k-steps of
-// 8 rests; its fragments come straight from the swizzled tile (no staging):
-// lane (g, t) reads rows/columns g and g + 8 at rests 8 s + t and 8 s + t + 4.
-// Accumulators: acc[nt][0] = Re, acc[nt][1] = Zr Xi^T, acc[nt][2] = Zi Xr^T
-// for the column tiles nt = 0 (entries 0..7) and 1 (8..15).
+// Each fp32 operand v is split v = hi + lo with hi = v rounded to the
+// 10-bit tf32 mantissa (round half away from zero on the bit pattern) and
+// lo = v - hi, exact in fp32 with |lo| <= 2^-11 |v|; the tensor core reads
+// lo truncated to tf32 (it ignores the low 13 bits of a tf32 operand).  A
+// product is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32
+// scheme), which leaves a relative error below about 2^-20 per product.
+// A warp owns k-steps of 8 rests; its fragments come straight from the
+// swizzled tile (no staging): lane (g, t) reads rows/columns g and g + 8 at
+// rests 8 s + t and 8 s + t + 4.  Accumulators, for the column tiles nt = 0
+// (entries 0..7) and 1 (8..15): acc[nt][0] = Zr Xr^T, acc[nt][1] = Zr Xi^T,
+// acc[nt][2] = Zi Xr^T, acc[nt][3] = Zi Xi^T (four independent chains).
 __device__ __forceinline__ void tf32_split(float v, unsigned& hi, unsigned& lo) {
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(hi) : "f"(v));
-  const float r = v - __uint_as_float(hi);
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(lo) : "f"(r));
+  hi = (__float_as_uint(v) + 0x1000u) & 0xffffe000u;
+  lo = __float_as_uint(v - __uint_as_float(hi));
 }
 
 __device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
@@ -324,7 +354,7 @@ __device__ __forceinline__ void mma3(float (&c)[4], const unsigned (&ah)[4], con
 
 // Needs 2^(T - 4) >= 8 rests.
 __device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2* xs, const float2* zs,
-                                              float (&acc)[2][3][4]) {
+                                              float (&acc)[2][4][4]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const int w0 = sh.wl[gq], w1 = sh.wl[gq + 8];
@@ -356,16 +386,120 @@ __device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt) {
       mma3(acc[nt][0], zrh, zrl, xrh[nt], xrl[nt]);
-      mma3(acc[nt][0], zih, zil, xih[nt], xil[nt]);
       mma3(acc[nt][1], zrh, zrl, xih[nt], xil[nt]);
       mma3(acc[nt][2], zih, zil, xrh[nt], xrl[nt]);
+      mma3(acc[nt][3], zih, zil, xih[nt], xil[nt]);
     }
   }
 }
 
+// Previous group's peels on x and new gates on z on the tensor cores.  The
+// group's gates of each side are composed into one 16 x 16 matrix G
+// (compose_gates, once per chunk) and V <- G V for the 16 x position matrix
+// V of the tile over the previous window, as 3xTF32 m16n8k8 products:
+//   Re V' = Gr Vr + (-Gi) Vi,   Im V' = Gr Vi + Gi Vr.
+// A warp owns column tiles of 8 positions; all of its loads come before its
+// stores and no other warp touches its positions.  Needs 2^(T - 4) >= 8.
+static_assert(PASS_THREADS / 32 * 4 >= (1 << (GT - 7)), "four column tiles per warp cover a tile");
+__device__ __forceinline__ void pass_apply_tc(const PassShared& sh, float2* xs, float2* zs) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const int nnt = 1 << (sh.T - 7), npos = 1 << (sh.T - 4);   // column tiles, positions of the tile
+  for (int side = 0; side < 2; ++side) {
+    float2* v = side ? zs : xs;
+    float c[4][2][4];   // [column tile of this warp][Re, Im][fragment]
+#pragma unroll
+    for (int e = 0; e < 32; ++e) (&c[0][0][0])[e] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+      const uint4 frh = sh.gf[side][ks][0][lane], frl = sh.gf[side][ks][1][lane];
+      const uint4 fih = sh.gf[side][ks][2][lane], fil = sh.gf[side][ks][3][lane];
+      const unsigned grh[4] = {frh.x, frh.y, frh.z, frh.w}, grl[4] = {frl.x, frl.y, frl.z, frl.w};
+      const unsigned gih[4] = {fih.x, fih.y, fih.z, fih.w}, gil[4] = {fil.x, fil.y, fil.z, fil.w};
+      unsigned ngih[4], ngil[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        ngih[i] = gih[i] ^ 0x80000000u;
+        ngil[i] = gil[i] ^ 0x80000000u;
+      }
+      const int wa = sh.wlp[8 * ks + tq], wb = sh.wlp[8 * ks + tq + 4];
+      // column tiles past the tile's positions (T < GT) read wrapped
+      // positions and are not stored
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nt = warp + j * nwarps;
+        const int po = sh.plp[(8 * nt + gq) & (npos - 1)];
+        // b0 = V[8 ks + t][8 nt + g], b1 = V[8 ks + t + 4][8 nt + g]
+        const float2 v0 = v[wa ^ po], v1 = v[wb ^ po];
+        unsigned rh[2], rl[2], ih[2], il[2];
+        tf32_split(v0.x, rh[0], rl[0]);
+        tf32_split(v1.x, rh[1], rl[1]);
+        tf32_split(v0.y, ih[0], il[0]);
+        tf32_split(v1.y, ih[1], il[1]);
+        mma3(c[j][0], grh, grl, rh, rl);
+        mma3(c[j][1], grh, grl, ih, il);
+        mma3(c[j][0], ngih, ngil, ih, il);
+        mma3(c[j][1], gih, gil, rh, rl);
+      }
+    }
+    // c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
+    const int w0 = sh.wlp[gq], w1 = sh.wlp[gq + 8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int nt = warp + j * nwarps;
+      if (nt >= nnt) continue;
+      const int p0 = sh.plp[8 * nt + 2 * tq], p1 = sh.plp[8 * nt + 2 * tq + 1];
+      v[w0 ^ p0] = cf(c[j][0][0], c[j][1][0]);
+      v[w0 ^ p1] = cf(c[j][0][1], c[j][1][1]);
+      v[w1 ^ p0] = cf(c[j][0][2], c[j][1][2]);
+      v[w1 ^ p1] = cf(c[j][0][3], c[j][1][3]);
+    }
+  }
+}
+
+// Compose the previous group's gates of each side into G (threads 0-31:
+// side t / 16, column t % 16, written to `scratch` as [side][row][col]),
+// then split G into the A fragments of pass_apply_tc (one thread per side,
+// k-step and lane).  `scratch` aliases the tile buffers.
+__device__ __forceinline__ void compose_gates(PassShared& sh, float2* scratch) {
+  const int t = threadIdx.x;
+  if (t < 32) {
+    const int side = t >> 4, col = t & 15;
+    float2 a[16];
+#pragma unroll
+    for (int w = 0; w < 16; ++w) a[w] = cf(w == col ? 1.f : 0.f, 0.f);
+    for (int s = 0; s < sh.npk; ++s)
+      if (sh.pk[s]) win_apply<4>(a, sh.gm[side][s], sh.pk[s], sh.phi[s], sh.plo[s]);
+#pragma unroll
+    for (int w = 0; w < 16; ++w) scratch[side * 256 + w * 16 + col] = a[w];
+  }
+  __syncthreads();
+  for (int e = t; e < 2 * 2 * 32; e += blockDim.x) {
+    const int side = e >> 6, ks = (e >> 5) & 1, lane = e & 31, gq = lane >> 2, tq = lane & 3;
+    // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4) of the k-step
+    const float2* G = scratch + side * 256;
+    const float2 g0 = G[gq * 16 + 8 * ks + tq], g1 = G[(gq + 8) * 16 + 8 * ks + tq];
+    const float2 g2 = G[gq * 16 + 8 * ks + tq + 4], g3 = G[(gq + 8) * 16 + 8 * ks + tq + 4];
+    uint4 rh, rl, ih, il;
+    tf32_split(g0.x, rh.x, rl.x);
+    tf32_split(g1.x, rh.y, rl.y);
+    tf32_split(g2.x, rh.z, rl.z);
+    tf32_split(g3.x, rh.w, rl.w);
+    tf32_split(g0.y, ih.x, il.x);
+    tf32_split(g1.y, ih.y, il.y);
+    tf32_split(g2.y, ih.z, il.z);
+    tf32_split(g3.y, ih.w, il.w);
+    sh.gf[side][ks][0][lane] = rh;
+    sh.gf[side][ks][1][lane] = rl;
+    sh.gf[side][ks][2][lane] = ih;
+    sh.gf[side][ks][3][lane] = il;
+  }
+  __syncthreads();
+}
+
 // Sum the warps' M (fixed order) into the chunk's partial.  `red` aliases
 // the tile buffers (needs nwarps * 256 double2).
-__device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][3][4], double2* red, double2* out) {
+__device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][4][4], double2* red, double2* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   __syncthreads();   // tile buffers free
@@ -375,7 +509,7 @@ __device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][3][4], doubl
     for (int e = 0; e < 4; ++e) {
       const int i = gq + (e >> 1) * 8, k = nt * 8 + 2 * tq + (e & 1);
       red[warp * GMM + i * GM + k] =
-          cd((double)acc[nt][0][e], (double)acc[nt][1][e] - (double)acc[nt][2][e]);
+          cd((double)acc[nt][0][e] + (double)acc[nt][3][e], (double)acc[nt][1][e] - (double)acc[nt][2][e]);
     }
   __syncthreads();
   for (int ent = threadIdx.x; ent < GMM; ent += blockDim.x) {
@@ -463,11 +597,11 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
   const float2* zv_in = z_in + bd.vec_off[b];
   float2* zv_out = z_out + bd.vec_off[b];
   float2 acc[TC ? 1 : 16];
-  float tacc[2][3][4];
+  float tacc[2][4][4];
 #pragma unroll
   for (int e = 0; e < (TC ? 1 : 16); ++e) acc[e] = cf(0.f, 0.f);
 #pragma unroll
-  for (int e = 0; e < 24; ++e) (&tacc[0][0][0])[e] = 0.f;
+  for (int e = 0; e < 32; ++e) (&tacc[0][0][0])[e] = 0.f;
   const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
   const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
   int64_t base = deposit_bits(t0, rest_mask);
@@ -477,7 +611,8 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
     cp_async_wait<0>();
     __syncthreads();
     if (g > 0) {
-      pass_apply<U>(sh, xs, zs);
+      if constexpr (TC) pass_apply_tc(sh, xs, zs);
+      else pass_apply<U>(sh, xs, zs);
       __syncthreads();
       pass_store(sh, xv + base, zv_out + base, xs, zs);
     }
@@ -561,7 +696,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
     }
     for (int r = threadIdx.x; r < (1 << (T - U)); r += blockDim.x) {
       sh.rl[r] = swz(rest_offset(r, sh.wml_c, full & ~sh.wml_c));
-      sh.plp[r] = swz(deposit32(r, full & ~sh.wml_p));
+      sh.plp[r] = swz(U == 4 && T >= 7 ? apply_pos_offset(r, sh.wml_p, full & ~sh.wml_p)
+                                        : deposit32(r, full & ~sh.wml_p));
     }
     if (g > 0) {
       // stage P = (new gate)^H and Q = (replaced gate)^H of each previous
@@ -582,6 +718,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       }
     }
     __syncthreads();
+    if (U == 4 && T >= 7 && g > 0) compose_gates(sh, xs);
     if (U == 4 && T >= 7) pass_chunk<4, true>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 4) pass_chunk<4, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 3) pass_chunk<3, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);

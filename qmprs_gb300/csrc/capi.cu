@@ -696,7 +696,8 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
   if (rc != QMPRS_OK) return rc;
   const signed char* ar = (const signed char*)arity;
   // C|0> with the rebuild passes of the sweep: two 4-qubit windows of
-  // consecutive gates per pass
+  // consecutive gates per pass, in fp32 FMAs (the reported state, so not
+  // the split-precision tensor-core products of the sweep's rebuild)
   launch_group_plan(p->bd, p->gd, ar, num_layers, s);
   std::vector<int> nrgroups(p->B, 0);
   CK(cudaMemcpyAsync(nrgroups.data(), p->d_nrgroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
@@ -706,7 +707,7 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
   float2* psi = (float2*)out;
   launch_set_zero_state(p->bd, psi, nullptr, s);
   for (int r = 0; r < passes; ++r)
-    launch_rebuild_pass(p->bd, p->gd, r, psi, (const double2*)gates, ar, num_layers, nullptr, s);
+    launch_rebuild_pass(p->bd, p->gd, r, psi, (const double2*)gates, ar, num_layers, nullptr, s, ORDER_FWD, 0, true);
   CK(cudaGetLastError());
   return QMPRS_OK;
 }
@@ -728,7 +729,8 @@ int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t
   const signed char* ar = (const signed char*)arity;
   launch_layer_plan(p->bd, p->gd, ar, mode, layer, nullptr, s);
   for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
-    launch_rebuild_pass(p->bd, p->gd, r, (float2*)vec, (const double2*)gates, ar, nullptr, nullptr, s, mode, layer);
+    launch_rebuild_pass(p->bd, p->gd, r, (float2*)vec, (const double2*)gates, ar, nullptr, nullptr, s, mode, layer,
+                        true);
   CK(cudaGetLastError());
   return QMPRS_OK;
 }

@@ -156,7 +156,7 @@ void launch_group_plan(const BatchDev& bd, const GroupDev& gd, const signed char
 enum { ORDER_BWD = 0, ORDER_FWD = 1, ORDER_LAYER_INV = 2, ORDER_LAYER_FWD = 3 };
 void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
                          const signed char* arity, const int* nlayers, const int* active, cudaStream_t s,
-                         int mode = ORDER_FWD, int layer = 0);
+                         int mode = ORDER_FWD, int layer = 0, bool exact = false);
 void launch_layer_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, int mode, int layer,
                        const int* active, cudaStream_t s);
 int layer_pass_bound(int max_n);

@@ -323,10 +323,12 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
 //   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T.
 // Each fp32 operand v is split v = hi + lo with hi = v rounded to the
 // 10-bit tf32 mantissa (round half away from zero on the bit pattern) and
-// lo = v - hi, exact in fp32 with |lo| <= 2^-11 |v|; the tensor core reads
-// lo truncated to tf32 (it ignores the low 13 bits of a tf32 operand).  A
-// product is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32
-// scheme), which leaves a relative error below about 2^-20 per product.
+// lo = v - hi, exact in fp32 with |lo| <= 2^-11 |v|.  The tensor core
+// ignores the low 13 bits of a tf32 operand, so lo is passed with half a
+// tf32 ulp added to its bit pattern, which rounds it to nearest.  A product
+// is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32 scheme): the
+// dropped lo_a lo_b and the rounding of lo leave a relative error of at most
+// 3 * 2^-22 per product.
 // A warp owns k-steps of 8 rests; its fragments come straight from the
 // swizzled tile (no staging): lane (g, t) reads rows/columns g and g + 8 at
 // rests 8 s + t and 8 s + t + 4.  Accumulators, for the column tiles nt = 0
@@ -334,7 +336,7 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
 // acc[nt][2] = Zi Xr^T, acc[nt][3] = Zi Xi^T (four independent chains).
 __device__ __forceinline__ void tf32_split(float v, unsigned& hi, unsigned& lo) {
   hi = (__float_as_uint(v) + 0x1000u) & 0xffffe000u;
-  lo = __float_as_uint(v - __uint_as_float(hi));
+  lo = __float_as_uint(v - __uint_as_float(hi)) + 0x1000u;
 }
 
 __device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
@@ -393,91 +395,106 @@ __device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2
   }
 }
 
-// Previous group's peels on x and new gates on z on the tensor cores.  The
-// group's gates of each side are composed into one 16 x 16 matrix G
-// (compose_gates, once per chunk) and V <- G V for the 16 x position matrix
-// V of the tile over the previous window, as 3xTF32 m16n8k8 products:
-//   Re V' = Gr Vr + (-Gi) Vi,   Im V' = Gr Vi + Gi Vr.
-// A warp owns column tiles of 8 positions; all of its loads come before its
-// stores and no other warp touches its positions.  Needs 2^(T - 4) >= 8.
+// V <- G V on the tensor cores, with V the 16 x position matrix of a tile
+// over a 4-qubit window (wlt: window entry -> tile offset, plt: position ->
+// tile offset) and G given as the A fragments `gf` of compose_gates:
+//   Re V' = Gr Vr + (-Gi) Vi,   Im V' = Gr Vi + Gi Vr
+// as 3xTF32 m16n8k8 products.  A warp owns column tiles of 8 positions; all
+// of its loads come before its stores and no other warp touches its
+// positions.  Needs 2^(T - 4) >= 8.
 static_assert(PASS_THREADS / 32 * 4 >= (1 << (GT - 7)), "four column tiles per warp cover a tile");
-__device__ __forceinline__ void pass_apply_tc(const PassShared& sh, float2* xs, float2* zs) {
+__device__ __forceinline__ void tile_apply_tc(const int* wlt, const int* plt, const uint4 (*gf)[4][32], int T,
+                                              float2* v) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
-  const int nnt = 1 << (sh.T - 7), npos = 1 << (sh.T - 4);   // column tiles, positions of the tile
-  for (int side = 0; side < 2; ++side) {
-    float2* v = side ? zs : xs;
-    float c[4][2][4];   // [column tile of this warp][Re, Im][fragment]
+  const int nnt = 1 << (T - 7), npos = 1 << (T - 4);   // column tiles, positions of the tile
+  float c[4][2][4];   // [column tile of this warp][Re, Im][fragment]
 #pragma unroll
-    for (int e = 0; e < 32; ++e) (&c[0][0][0])[e] = 0.f;
+  for (int e = 0; e < 32; ++e) (&c[0][0][0])[e] = 0.f;
 #pragma unroll
-    for (int ks = 0; ks < 2; ++ks) {
-      const uint4 frh = sh.gf[side][ks][0][lane], frl = sh.gf[side][ks][1][lane];
-      const uint4 fih = sh.gf[side][ks][2][lane], fil = sh.gf[side][ks][3][lane];
-      const unsigned grh[4] = {frh.x, frh.y, frh.z, frh.w}, grl[4] = {frl.x, frl.y, frl.z, frl.w};
-      const unsigned gih[4] = {fih.x, fih.y, fih.z, fih.w}, gil[4] = {fil.x, fil.y, fil.z, fil.w};
-      unsigned ngih[4], ngil[4];
+  for (int ks = 0; ks < 2; ++ks) {
+    const uint4 frh = gf[ks][0][lane], frl = gf[ks][1][lane];
+    const uint4 fih = gf[ks][2][lane], fil = gf[ks][3][lane];
+    const unsigned grh[4] = {frh.x, frh.y, frh.z, frh.w}, grl[4] = {frl.x, frl.y, frl.z, frl.w};
+    const unsigned gih[4] = {fih.x, fih.y, fih.z, fih.w}, gil[4] = {fil.x, fil.y, fil.z, fil.w};
+    unsigned ngih[4], ngil[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        ngih[i] = gih[i] ^ 0x80000000u;
-        ngil[i] = gil[i] ^ 0x80000000u;
-      }
-      const int wa = sh.wlp[8 * ks + tq], wb = sh.wlp[8 * ks + tq + 4];
-      // column tiles past the tile's positions (T < GT) read wrapped
-      // positions and are not stored
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int nt = warp + j * nwarps;
-        const int po = sh.plp[(8 * nt + gq) & (npos - 1)];
-        // b0 = V[8 ks + t][8 nt + g], b1 = V[8 ks + t + 4][8 nt + g]
-        const float2 v0 = v[wa ^ po], v1 = v[wb ^ po];
-        unsigned rh[2], rl[2], ih[2], il[2];
-        tf32_split(v0.x, rh[0], rl[0]);
-        tf32_split(v1.x, rh[1], rl[1]);
-        tf32_split(v0.y, ih[0], il[0]);
-        tf32_split(v1.y, ih[1], il[1]);
-        mma3(c[j][0], grh, grl, rh, rl);
-        mma3(c[j][1], grh, grl, ih, il);
-        mma3(c[j][0], ngih, ngil, ih, il);
-        mma3(c[j][1], gih, gil, rh, rl);
-      }
+    for (int i = 0; i < 4; ++i) {
+      ngih[i] = gih[i] ^ 0x80000000u;
+      ngil[i] = gil[i] ^ 0x80000000u;
     }
-    // c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
-    const int w0 = sh.wlp[gq], w1 = sh.wlp[gq + 8];
+    const int wa = wlt[8 * ks + tq], wb = wlt[8 * ks + tq + 4];
+    // column tiles past the tile's positions (T < GT) read wrapped
+    // positions and are not stored
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int nt = warp + j * nwarps;
-      if (nt >= nnt) continue;
-      const int p0 = sh.plp[8 * nt + 2 * tq], p1 = sh.plp[8 * nt + 2 * tq + 1];
-      v[w0 ^ p0] = cf(c[j][0][0], c[j][1][0]);
-      v[w0 ^ p1] = cf(c[j][0][1], c[j][1][1]);
-      v[w1 ^ p0] = cf(c[j][0][2], c[j][1][2]);
-      v[w1 ^ p1] = cf(c[j][0][3], c[j][1][3]);
+      const int po = plt[(8 * nt + gq) & (npos - 1)];
+      // b0 = V[8 ks + t][8 nt + g], b1 = V[8 ks + t + 4][8 nt + g]
+      const float2 v0 = v[wa ^ po], v1 = v[wb ^ po];
+      unsigned rh[2], rl[2], ih[2], il[2];
+      tf32_split(v0.x, rh[0], rl[0]);
+      tf32_split(v1.x, rh[1], rl[1]);
+      tf32_split(v0.y, ih[0], il[0]);
+      tf32_split(v1.y, ih[1], il[1]);
+      mma3(c[j][0], grh, grl, rh, rl);
+      mma3(c[j][1], grh, grl, ih, il);
+      mma3(c[j][0], ngih, ngil, ih, il);
+      mma3(c[j][1], gih, gil, rh, rl);
     }
+  }
+  // c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
+  const int w0 = wlt[gq], w1 = wlt[gq + 8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int nt = warp + j * nwarps;
+    if (nt >= nnt) continue;
+    const int p0 = plt[8 * nt + 2 * tq], p1 = plt[8 * nt + 2 * tq + 1];
+    v[w0 ^ p0] = cf(c[j][0][0], c[j][1][0]);
+    v[w0 ^ p1] = cf(c[j][0][1], c[j][1][1]);
+    v[w1 ^ p0] = cf(c[j][0][2], c[j][1][2]);
+    v[w1 ^ p1] = cf(c[j][0][3], c[j][1][3]);
   }
 }
 
-// Compose the previous group's gates of each side into G (threads 0-31:
-// side t / 16, column t % 16, written to `scratch` as [side][row][col]),
-// then split G into the A fragments of pass_apply_tc (one thread per side,
-// k-step and lane).  `scratch` aliases the tile buffers.
-__device__ __forceinline__ void compose_gates(PassShared& sh, float2* scratch) {
+// Previous group's peels on x and new gates on z (pass kernel).
+__device__ __forceinline__ void pass_apply_tc(const PassShared& sh, float2* xs, float2* zs) {
+  tile_apply_tc(sh.wlp, sh.plp, sh.gf[0], sh.T, xs);
+  tile_apply_tc(sh.wlp, sh.plp, sh.gf[1], sh.T, zs);
+}
+
+// The gate steps of one window: step s applies the row-major matrix gm[s]
+// (arity pk[s], 0 = skip) on window bits (phi[s], plo[s]).
+struct GateList {
+  const int *pk, *phi, *plo;
+  const float2 (*gm)[16];
+  int n;
+};
+
+// Compose up to two gate lists into 16 x 16 matrices G (threads 0-31:
+// matrix t / 16, column t % 16, written to `scratch` as [matrix][row][col])
+// and split G into the A fragments of tile_apply_tc (one thread per matrix,
+// k-step and lane).  `scratch` aliases the tile buffers; the block must call
+// this uniformly.
+__device__ __forceinline__ void compose_gates(const GateList (&gl)[2], int nmat, float2* scratch,
+                                              uint4 (*gf)[2][4][32]) {
   const int t = threadIdx.x;
-  if (t < 32) {
-    const int side = t >> 4, col = t & 15;
+  if (t < 16 * nmat) {
+    const int m = t >> 4, col = t & 15;
+    const GateList g = m ? gl[1] : gl[0];
     float2 a[16];
 #pragma unroll
     for (int w = 0; w < 16; ++w) a[w] = cf(w == col ? 1.f : 0.f, 0.f);
-    for (int s = 0; s < sh.npk; ++s)
-      if (sh.pk[s]) win_apply<4>(a, sh.gm[side][s], sh.pk[s], sh.phi[s], sh.plo[s]);
+    for (int s = 0; s < g.n; ++s)
+      if (g.pk[s]) win_apply<4>(a, g.gm[s], g.pk[s], g.phi[s], g.plo[s]);
 #pragma unroll
-    for (int w = 0; w < 16; ++w) scratch[side * 256 + w * 16 + col] = a[w];
+    for (int w = 0; w < 16; ++w) scratch[m * 256 + w * 16 + col] = a[w];
   }
   __syncthreads();
-  for (int e = t; e < 2 * 2 * 32; e += blockDim.x) {
-    const int side = e >> 6, ks = (e >> 5) & 1, lane = e & 31, gq = lane >> 2, tq = lane & 3;
+  for (int e = t; e < nmat * 2 * 32; e += blockDim.x) {
+    const int m = e >> 6, ks = (e >> 5) & 1, lane = e & 31, gq = lane >> 2, tq = lane & 3;
     // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4) of the k-step
-    const float2* G = scratch + side * 256;
+    const float2* G = scratch + m * 256;
     const float2 g0 = G[gq * 16 + 8 * ks + tq], g1 = G[(gq + 8) * 16 + 8 * ks + tq];
     const float2 g2 = G[gq * 16 + 8 * ks + tq + 4], g3 = G[(gq + 8) * 16 + 8 * ks + tq + 4];
     uint4 rh, rl, ih, il;
@@ -489,10 +506,10 @@ __device__ __forceinline__ void compose_gates(PassShared& sh, float2* scratch) {
     tf32_split(g1.y, ih.y, il.y);
     tf32_split(g2.y, ih.z, il.z);
     tf32_split(g3.y, ih.w, il.w);
-    sh.gf[side][ks][0][lane] = rh;
-    sh.gf[side][ks][1][lane] = rl;
-    sh.gf[side][ks][2][lane] = ih;
-    sh.gf[side][ks][3][lane] = il;
+    gf[m][ks][0][lane] = rh;
+    gf[m][ks][1][lane] = rl;
+    gf[m][ks][2][lane] = ih;
+    gf[m][ks][3][lane] = il;
   }
   __syncthreads();
 }
@@ -718,7 +735,10 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       }
     }
     __syncthreads();
-    if (U == 4 && T >= 7 && g > 0) compose_gates(sh, xs);
+    if (U == 4 && T >= 7 && g > 0) {
+      const GateList gl[2] = {{sh.pk, sh.phi, sh.plo, sh.gm[0], sh.npk}, {sh.pk, sh.phi, sh.plo, sh.gm[1], sh.npk}};
+      compose_gates(gl, 2, xs, sh.gf);
+    }
     if (U == 4 && T >= 7) pass_chunk<4, true>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 4) pass_chunk<4, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 3) pass_chunk<3, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
@@ -742,6 +762,7 @@ struct RebuildShared {
   int pl[2][1 << (GT - GW)];       // position -> swizzled tile offset
   int d0[64], d1[64];
   float2 gm[2][GMAXSTEPS][16];     // the gates, row-major complex
+  uint4 gf[2][2][4][32];           // [window][k-step][Gr hi, Gr lo, Gi hi, Gi lo][lane]: tensor-core A fragments
 };
 
 template <int U>
@@ -759,9 +780,11 @@ __device__ __forceinline__ void rebuild_apply(const RebuildShared& sh, int w, fl
   }
 }
 
-template <int U>
+// TC: the windows' gates on the tensor cores (U = 4, T >= 7).
+template <int U, bool TC>
 __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev& gd, const RebuildShared& sh,
                                               float2* xs, int b, int chunk, float2* psi) {
+  static_assert(!TC || U == 4, "tensor-core windows need 16 entries");
   const int n = bd.n[b];
   const int64_t ntiles = (int64_t)1 << (n - sh.T);
   const int64_t rest_mask = (((int64_t)1 << n) - 1) & ~(int64_t)sh.pos_mask;
@@ -776,7 +799,8 @@ __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev
     cp_async_wait<0>();
     __syncthreads();
     for (int w = 0; w < sh.nw; ++w) {
-      rebuild_apply<U>(sh, w, xs);
+      if constexpr (TC) tile_apply_tc(sh.wl[w], sh.pl[w], sh.gf[w], sh.T, xs);
+      else rebuild_apply<U>(sh, w, xs);
       __syncthreads();
     }
     for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x)
@@ -792,7 +816,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
                                                                                  const signed char* arity,
                                                                                  const int* nlayers,
                                                                                  const int* active, int mode,
-                                                                                 int layer) {
+                                                                                 int layer, bool exact) {
   extern __shared__ __align__(16) unsigned char dyn[];
   float2* xs = reinterpret_cast<float2*>(dyn);
   __shared__ RebuildShared sh;
@@ -859,7 +883,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
     }
     for (int t = threadIdx.x; t < 2 * (1 << (T - U)); t += blockDim.x) {
       const int w = t / (1 << (T - U)), r = t % (1 << (T - U));
-      sh.pl[w][r] = swz(deposit32(r, full & ~sh.wm[w]));
+      sh.pl[w][r] = swz(U == 4 && T >= 7 && !exact ? apply_pos_offset(r, sh.wm[w], full & ~sh.wm[w])
+                                         : deposit32(r, full & ~sh.wm[w]));
     }
     for (int t = threadIdx.x; t < 2 * GMAXSTEPS * 16; t += blockDim.x) {
       const int w = t / (GMAXSTEPS * 16), st = (t / 16) % GMAXSTEPS, e = t % 16;
@@ -875,9 +900,14 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
       sh.gm[w][st][e] = cf((float)v.x, (float)v.y);
     }
     __syncthreads();
-    if (U == 4) rebuild_chunk<4>(bd, gd, sh, xs, b, chunk, psi);
-    else if (U == 3) rebuild_chunk<3>(bd, gd, sh, xs, b, chunk, psi);
-    else rebuild_chunk<2>(bd, gd, sh, xs, b, chunk, psi);
+    if (U == 4 && T >= 7 && !exact) {
+      const GateList gl[2] = {{sh.pk[0], sh.phi[0], sh.plo[0], sh.gm[0], sh.nst[0]},
+                              {sh.pk[1], sh.phi[1], sh.plo[1], sh.gm[1], sh.nst[1]}};
+      compose_gates(gl, nw, xs, sh.gf);
+      rebuild_chunk<4, true>(bd, gd, sh, xs, b, chunk, psi);
+    } else if (U == 4) rebuild_chunk<4, false>(bd, gd, sh, xs, b, chunk, psi);
+    else if (U == 3) rebuild_chunk<3, false>(bd, gd, sh, xs, b, chunk, psi);
+    else rebuild_chunk<2, false>(bd, gd, sh, xs, b, chunk, psi);
   }
 }
 
@@ -1077,12 +1107,12 @@ int layer_pass_bound(int max_n) {
 
 void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
                          const signed char* arity, const int* nlayers, const int* active, cudaStream_t s, int mode,
-                         int layer) {
+                         int layer, bool exact) {
   int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
   if (grid < 1) grid = 1;
   qm_note_launch();
   k_rebuild_pass<<<grid, PASS_THREADS, (size_t)sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
-                                                                          nlayers, active, mode, layer);
+                                                                          nlayers, active, mode, layer, exact);
 }
 
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,

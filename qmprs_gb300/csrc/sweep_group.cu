@@ -321,22 +321,25 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
 // m16n8k8 TF32 products (rows: window entry of z, columns: window entry of
 // x, reduction: rests):
 //   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T.
-// Each fp32 operand v is split v = hi + lo with hi = v rounded to the
-// 10-bit tf32 mantissa (round half away from zero on the bit pattern) and
-// lo = v - hi, exact in fp32 with |lo| <= 2^-11 |v|.  The tensor core
-// ignores the low 13 bits of a tf32 operand, so lo is passed with half a
-// tf32 ulp added to its bit pattern, which rounds it to nearest.  A product
-// is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b (the 3xTF32 scheme): the
-// dropped lo_a lo_b and the rounding of lo leave a relative error of at most
-// 3 * 2^-22 per product.
+// Each fp32 operand v is split v = hi + lo by Veltkamp's splitting
+// (multiply by 2^13 + 1): hi is v rounded to nearest with 11 significant
+// bits, the tf32 precision, and lo = v - hi is exact with at most 12
+// significant bits and |lo| <= 2^-11 |v|.  The tensor core ignores the low
+// 13 bits of a tf32 operand, so it reads hi exactly and lo truncated by at
+// most one bit.  A product is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b
+// (the 3xTF32 scheme): the dropped lo_a lo_b and the truncation of lo leave
+// a relative error of at most 3 * 2^-22 per product.  The split runs on the
+// FP32 pipe (explicitly rounded operations, no contraction).
 // A warp owns k-steps of 8 rests; its fragments come straight from the
 // swizzled tile (no staging): lane (g, t) reads rows/columns g and g + 8 at
 // rests 8 s + t and 8 s + t + 4.  Accumulators, for the column tiles nt = 0
 // (entries 0..7) and 1 (8..15): acc[nt][0] = Zr Xr^T, acc[nt][1] = Zr Xi^T,
 // acc[nt][2] = Zi Xr^T, acc[nt][3] = Zi Xi^T (four independent chains).
 __device__ __forceinline__ void tf32_split(float v, unsigned& hi, unsigned& lo) {
-  hi = (__float_as_uint(v) + 0x1000u) & 0xffffe000u;
-  lo = __float_as_uint(v - __uint_as_float(hi)) + 0x1000u;
+  const float g = __fmul_rn(v, 8193.f);
+  const float h = __fsub_rn(g, __fsub_rn(g, v));
+  hi = __float_as_uint(h);
+  lo = __float_as_uint(__fsub_rn(v, h));
 }
 
 __device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
@@ -555,15 +558,16 @@ __device__ __forceinline__ void cp_async_wait() {
 #define PASS_PER ((1 << GT) / PASS_THREADS)
 static_assert(PASS_THREADS % 64 == 0 && (1 << GT) % PASS_THREADS == 0, "full-tile index split");
 
+// swz(t + PASS_THREADS u) = swz(t) ^ swz(PASS_THREADS u) for t < PASS_THREADS
+// (disjoint bits), the second term a constant of the unrolled loop.
 __device__ __forceinline__ void pass_issue(const PassShared& sh, const float2* xg, const float2* zg, float2* xs,
                                            float2* zs) {
   if (sh.T == GT) {
-    const int t = threadIdx.x, lo = sh.d0[t & 63];
+    const int t = threadIdx.x, lo = sh.d0[t & 63], st = swz(t);
 #pragma unroll
     for (int u = 0; u < PASS_PER; ++u) {
-      const int li = t + u * PASS_THREADS;
       const int o = lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)];
-      const int sl = swz(li);
+      const int sl = st ^ swz(u * PASS_THREADS);
       cp_async8(xs + sl, xg + o);
       cp_async8(zs + sl, zg + o);
     }
@@ -579,12 +583,11 @@ __device__ __forceinline__ void pass_issue(const PassShared& sh, const float2* x
 __device__ __forceinline__ void pass_store(const PassShared& sh, float2* xg, float2* zg, const float2* xs,
                                            const float2* zs) {
   if (sh.T == GT) {
-    const int t = threadIdx.x, lo = sh.d0[t & 63];
+    const int t = threadIdx.x, lo = sh.d0[t & 63], st = swz(t);
 #pragma unroll
     for (int u = 0; u < PASS_PER; ++u) {
-      const int li = t + u * PASS_THREADS;
       const int o = lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)];
-      const int sl = swz(li);
+      const int sl = st ^ swz(u * PASS_THREADS);
       xg[o] = xs[sl];
       zg[o] = zs[sl];
     }
@@ -792,9 +795,17 @@ __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev
   const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
   const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
   int64_t base = deposit_bits(t0, rest_mask);
+  const int t = threadIdx.x, lo = sh.d0[t & 63], st = swz(t);
   for (int64_t tt = t0; tt < t1; ++tt) {
-    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x)
-      cp_async8(xs + swz(li), xv + base + (sh.d0[li & 63] | sh.d1[li >> 6]));
+    const float2* xg = xv + base;
+    if (sh.T == GT) {
+#pragma unroll
+      for (int u = 0; u < PASS_PER; ++u)
+        cp_async8(xs + (st ^ swz(u * PASS_THREADS)), xg + (lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]));
+    } else {
+      for (int li = t; li < (1 << sh.T); li += blockDim.x)
+        cp_async8(xs + swz(li), xg + (sh.d0[li & 63] | sh.d1[li >> 6]));
+    }
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -803,8 +814,14 @@ __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev
       else rebuild_apply<U>(sh, w, xs);
       __syncthreads();
     }
-    for (int li = threadIdx.x; li < (1 << sh.T); li += blockDim.x)
-      xv[base + (sh.d0[li & 63] | sh.d1[li >> 6])] = xs[swz(li)];
+    float2* xw = xv + base;
+    if (sh.T == GT) {
+#pragma unroll
+      for (int u = 0; u < PASS_PER; ++u)
+        xw[lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]] = xs[st ^ swz(u * PASS_THREADS)];
+    } else {
+      for (int li = t; li < (1 << sh.T); li += blockDim.x) xw[sh.d0[li & 63] | sh.d1[li >> 6]] = xs[swz(li)];
+    }
     __syncthreads();
     base = next_in_mask(base, rest_mask);
   }

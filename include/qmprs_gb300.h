@@ -95,6 +95,23 @@ int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, i
 int qmprs_plan_max_qubits(qmprs_plan_t p);
 
 /*
+ * Copy a packed complex64 statevector batch (`bytes` = vec_elems * 8, from
+ * host memory, ideally pinned) into the plan's own device input buffer on
+ * `stream` and return that buffer in *dev_out, ready for
+ * qmprs_mps_from_statevector and qmprs_overlap.  The buffer is allocated
+ * once, on the first call, and reused by later calls on the same plan; it
+ * lives until qmprs_plan_destroy.  Work that still reads it must be
+ * ordered before the next upload.  Pinned (device-mapped) host memory is
+ * read by a copy kernel on the SMs, which keeps many address translations
+ * in flight over the coherent host link; other host memory goes through
+ * cudaMemcpyAsync.
+ * Replaces: the host-to-device move of the input the reference leaves to
+ * its array library (qmprs/synthesis/mps_encoding/base.py:58-106 takes the
+ * statevector as a host array).
+ */
+int qmprs_plan_upload(qmprs_plan_t p, const void* host, int64_t bytes, void* stream, void** dev_out);
+
+/*
  * (a) Statevector -> MPS truncated to `max_bond` (<= the plan's), with the
  * quimb default cutoff `cutoff` (1e-10, rsum2).  Writes the site tensors
  * (l, p, r) of state b, site s at tensor_off[b] + s * 2 * chi_b^2 with

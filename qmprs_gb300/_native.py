@@ -41,6 +41,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmprs_plan_destroy": (None, [_c_void_p]),
     "qmprs_plan_layout": (ctypes.c_int, [_c_void_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p]),
     "qmprs_plan_max_qubits": (ctypes.c_int, [_c_void_p]),
+    "qmprs_plan_upload": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int64, _c_void_p, ctypes.POINTER(_c_void_p)]),
     "qmprs_mps_from_statevector": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, ctypes.c_double, _c_void_p,
                                                   _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_mps_to_statevector": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),

@@ -38,6 +38,7 @@ struct qmprs_plan {
   double2* tt_partials = nullptr;
   double2 *gram = nullptr, *vsel = nullptr, *vsel2 = nullptr, *vwork = nullptr;
   double2* site_t = nullptr;
+  float2* d_input = nullptr;   // qmprs_plan_upload's statevector batch (allocated on first use)
   int *bonds = nullptr, *active = nullptr, *nlayers = nullptr, *num_active = nullptr;
   double* nuc = nullptr;
   double2 *sq = nullptr, *tnorm = nullptr;
@@ -260,7 +261,7 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
                   p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials,
                   p->d_rgrp,   p->d_nrgroups,   p->d_wj_rot,  p->d_wj_count,  p->d_wj_perm,
-                  p->d_wj_trace, p->d_wj_lam};
+                  p->d_wj_trace, p->d_wj_lam, p->d_input};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -445,6 +446,25 @@ int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, i
 }
 
 int qmprs_plan_max_qubits(qmprs_plan_t p) { return p ? p->max_n : -1; }
+
+int qmprs_plan_upload(qmprs_plan_t p, const void* host, int64_t bytes, void* stream, void** dev_out) {
+  if (!p || !host || !dev_out) return QMPRS_ERR_INVALID;
+  *dev_out = nullptr;
+  if (bytes != p->vec_total * (int64_t)sizeof(float2))
+    return set_err(p->h, QMPRS_ERR_INVALID, "packed statevector buffer does not match the qubit counts");
+  if (!p->d_input) CK(cudaMalloc(&p->d_input, (size_t)bytes));
+  // Pinned, device-mapped host memory is read by a copy kernel (k_upload);
+  // anything else goes through the copy engine.
+  cudaPointerAttributes at{};
+  const bool mapped = cudaPointerGetAttributes(&at, host) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+                      at.devicePointer != nullptr && ((uintptr_t)at.devicePointer % 16) == 0 && bytes % 16 == 0;
+  cudaGetLastError();   // clear a failed query of pageable memory
+  if (mapped) launch_upload(p->d_input, at.devicePointer, bytes, (cudaStream_t)stream);
+  else CK(cudaMemcpyAsync(p->d_input, host, (size_t)bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  CK(cudaGetLastError());
+  *dev_out = p->d_input;
+  return QMPRS_OK;
+}
 
 int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, double cutoff, void* tensors_,
                                int* bonds, void* target_, void* stream) {

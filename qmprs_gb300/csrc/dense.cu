@@ -163,3 +163,23 @@ void launch_copy_normalize(const BatchDev& bd, const float2* src, float2* dst, d
   qm_note_launch();
   k_scale_copy<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, src, dst, sq);
 }
+
+// ---- input upload ---------------------------------------------------------------
+
+// Grid-stride copy of a pinned host buffer into device memory by the SMs
+// themselves: on a coherently attached host (NVLink-C2C) the loads go
+// straight to host memory, with the address translations of many SMs in
+// flight at once instead of one copy engine's.  16-byte words.
+__global__ void k_upload(float4* __restrict__ dst, const float4* __restrict__ src, int64_t n16) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+void launch_upload(void* dst, const void* src_dev, int64_t bytes, cudaStream_t s) {
+  const int64_t n16 = bytes / 16;
+  int64_t grid = (n16 + 255) / 256;
+  if (grid > 152 * 8) grid = 152 * 8;
+  if (grid < 1) grid = 1;
+  qm_note_launch();
+  k_upload<<<(int)grid, 256, 0, s>>>((float4*)dst, (const float4*)src_dev, n16);
+}

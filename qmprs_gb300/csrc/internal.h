@@ -130,6 +130,7 @@ struct GroupDev {
 // ---- launches (defined in the .cu files) ---------------------------------
 void launch_set_zero_state(const BatchDev& bd, float2* vec, const int* active, cudaStream_t s);
 void launch_apply_gate(const BatchDev& bd, float2* vec, const GateSel& sel, cudaStream_t s);
+void launch_upload(void* dst, const void* src_dev, int64_t bytes, cudaStream_t s);
 void launch_overlap(const BatchDev& bd, const float2* a, const float2* b, double2* partials,
                     double2* out, cudaStream_t s);
 void launch_copy_normalize(const BatchDev& bd, const float2* src, float2* dst, double2* partials,

@@ -61,6 +61,15 @@ def handle() -> Handle:
     return h
 
 
+class _DeviceBuffer:
+    """A float32 device array owned by the library (a plan buffer), exposed
+    to torch through the CUDA array interface without a copy."""
+
+    def __init__(self, ptr: int, numel: int):
+        self.__cuda_array_interface__ = {"shape": (int(numel),), "typestr": "<f4", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
 class Plan:
     """A batch layout: offsets of every state in the caller buffers."""
 
@@ -379,6 +388,30 @@ class Engine:
         st = stream or torch.cuda.current_stream()
         return ctypes.c_void_p(st.cuda_stream)
 
+    def _stage_input(self, p: Plan, host: torch.Tensor) -> torch.Tensor:
+        """Copy a packed host buffer into the plan's own device input buffer
+        (``qmprs_plan_upload``: one cudaMalloc per plan, reused) on the
+        current stream and return a tensor view of it.  The current stream
+        first waits for the previous call's last use of that buffer."""
+        if host.dtype != torch.float32 or not host.is_contiguous():
+            raise ValueError("packed statevectors must be a contiguous float32 tensor")
+        cur = torch.cuda.current_stream()
+        ev = getattr(p, "input_free", None)
+        if ev is not None:
+            cur.wait_event(ev)
+        dev = ctypes.c_void_p()
+        self.hd.check(self.lib.qmprs_plan_upload(p.p, ctypes.c_void_p(host.data_ptr()), host.numel() * 4,
+                                                 ctypes.c_void_p(cur.cuda_stream), ctypes.byref(dev)))
+        p.input_ptr = dev.value
+        return torch.as_tensor(_DeviceBuffer(dev.value, host.numel()), device="cuda")
+
+    @staticmethod
+    def _release_input(p: Plan, sv: torch.Tensor) -> None:
+        """Mark the end of this call's use of the plan's input buffer."""
+        if getattr(p, "input_ptr", None) == sv.data_ptr():
+            p.input_free = torch.cuda.Event()
+            p.input_free.record(torch.cuda.current_stream())
+
     # ---- whole path ------------------------------------------------------------
     def encode(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
                fidelity_threshold: float = 1 - 1e-6, stop_fidelity: float = 0.0,
@@ -405,7 +438,7 @@ class Engine:
             if sv.numel() != 2 * p.vec_elems:
                 raise ValueError("packed statevector buffer does not match the qubit counts")
             if not sv.is_cuda:
-                sv = sv.to("cuda", non_blocking=True)
+                sv = self._stage_input(p, sv)
         tensors, bonds, target = self.stage_mps(p, sv, bond_dimension)
         gates, arity, nl, lf = self.stage_layers(p, target, num_layers, fidelity_threshold)
         analytic = None
@@ -420,6 +453,7 @@ class Engine:
         if analytic is not None and stop_fidelity > 0.0:
             gates, sf, sd, ov = self._fallback(p, target, sv, analytic, gates, arity, nl, sf, sd, ov, nn,
                                                num_sweeps, stop_fidelity)
+        self._release_input(p, sv)
         B, S = p.B, max(int(num_sweeps), 0)
         if not download:
             return BatchResult(nqubits=p.nqubits, gates=gates, arity=arity, num_layers=nl, layer_fidelities=lf,

@@ -144,3 +144,26 @@ def test_layer_methods(api):
     assert abs(f_after) > abs(f_before)
     psi = D.apply_inverse_layer(sv, n, ref)
     assert abs(f_after - np.conj(psi[0])) < 1e-5
+
+
+def test_packed_host_input_matches_device(api):
+    """Packed complex64 batch from pinned host memory (qmprs_plan_upload into
+    the plan's input buffer, reused by the second call) gives bit-identical
+    results to the same batch resident on the device; a wrong size is
+    rejected."""
+    import torch
+    _, Sequential, Circuit = api
+    ns = [6, 9, 7]
+    svs = [S.uniform_complex(n, 40 + n).astype(np.complex64) for n in ns]
+    packed = np.concatenate([v.view(np.float32) for v in svs])
+    host = torch.from_numpy(packed).pin_memory()
+    dev = host.to("cuda")
+    cfg = dict(bond_dimension=16, num_layers=2, num_sweeps=2)
+    _, rd = Sequential(Circuit).prepare_states(dev, nqubits=ns, emit=False, **cfg)
+    for _ in range(2):
+        _, rh = Sequential(Circuit).prepare_states(host, nqubits=ns, emit=False, **cfg)
+        assert np.array_equal(rh.gates, rd.gates)
+        assert np.array_equal(rh.sweep_fidelities, rd.sweep_fidelities)
+        assert np.array_equal(rh.fidelity, rd.fidelity)
+    with pytest.raises(ValueError):
+        Sequential(Circuit).prepare_states(host[:-2], nqubits=ns, emit=False, **cfg)

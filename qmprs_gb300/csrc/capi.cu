@@ -684,7 +684,7 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
     for (int g = 0; g < max_groups; ++g) {
       log.begin(prof, s);
       const int e = launch_group_pass(p->bd, p->gd, g, psi, g <= 1 ? target : t, t, gates, ar, num_layers,
-                                      p->active, s);
+                                      p->active, p->tnorm, s);
       if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "cudaFuncSetAttribute(k_group_pass)");
       log.end(prof, 0, s);
       log.begin(prof, s);

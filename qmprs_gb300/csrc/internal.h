@@ -161,9 +161,10 @@ void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float
 void launch_layer_plan(const BatchDev& bd, const GroupDev& gd, const signed char* arity, int mode, int layer,
                        const int* active, cudaStream_t s);
 int layer_pass_bound(int max_n);
+// znorm: per-state <z|z> (x has unit norm), for the tensor-core scales
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
                       const double2* gates, const signed char* arity, const int* nlayers, const int* active,
-                      cudaStream_t s);
+                      const double2* znorm, cudaStream_t s);
 void launch_group_polar(const BatchDev& bd, const GroupDev& gd, int g, double2* gates, const signed char* arity,
                         const int* nlayers, const int* active, double* nuc, cudaStream_t s);
 void launch_sweep_finish(int B, int sweep, int num_sweeps, const double* nuc, const double2* tnorm2,

@@ -30,6 +30,8 @@
 // Group 0 only reads (x = C|0>, z = the target); group 1 reads the target
 // and writes t, so the target is never copied.  After the last group the
 // vectors are not needed: the sweep's fidelity is the last step's trace.
+#include <cuda_fp16.h>
+
 #include "window.cuh"
 
 // Gate of state b at backward step j: generated layer j / n, site
@@ -151,7 +153,8 @@ struct PassShared {
   int plp[1 << (GT - GW)];  // rest index -> swizzled tile offset (previous window)
   int d0[64], d1[64];       // global offset of tile index li: d0[li & 63] | d1[li >> 6]
   float2 gm[2][GMAXSTEPS][16];   // [peel | new][step]: the applied matrix, row-major complex
-  uint4 gf[2][2][4][32];    // [side][k-step][Gr hi, Gr lo, Gi hi, Gi lo][lane]: tensor-core A fragments
+  uint4 gf[2][6][32];       // [side][Gr hi, Gr lo, Gi hi, Gi lo, -Gi hi, -Gi lo][lane]: tensor-core A fragments
+  float sx, sz;             // tensor-core scales of x and z (powers of two)
 };
 
 // Dynamic shared memory: the tile of x and of z (float2 each).  Four blocks
@@ -175,60 +178,57 @@ __device__ __forceinline__ int deposit32(int v, int mask) {
   return r;
 }
 
-// Tile offset of rest index r.  Rest index bits 0 and 1 go to rest tile
-// bits whose bank residues (bit position mod 4: the swizzle folds tile bits
-// 4-7 and 8-11 onto 0-3) differ from each other and from those of the
-// window's two lowest bits, so that the 16 tensor-core fragment loads of a
-// half-warp (window entries 0-3 times rests 0-3) hit 16 distinct bank
-// pairs; the other rest bits follow in ascending order.  The reduction over
-// rests does not depend on their order.
 // bank residue (one-hot) of a single-bit mask; 0 for no bit
 __device__ __forceinline__ int bank_res(int bit) { return bit ? 1 << ((__ffs(bit) - 1) & 3) : 0; }
 
-// lowest bit of `left` whose residue is not in `avoid`, else 0
+// lowest bit of `left` whose residue is not in `avoid`, else the lowest bit
 __device__ __forceinline__ int pick_res(int left, int avoid) {
   for (int m = left; m; m &= m - 1) {
     const int bit = __ffs(m) - 1;
     if (!((avoid >> (bit & 3)) & 1)) return 1 << bit;
   }
-  return 0;
+  return left & (-left);
 }
 
-// residues of the two lowest bits of a window mask
-__device__ __forceinline__ int low2_res(int wmask) {
-  const int b0 = wmask & (-wmask), rest = wmask & ~b0;
-  return bank_res(b0) | bank_res(rest & (-rest));
+// the i-th lowest set bit of a mask (0 when it has fewer bits)
+__device__ __forceinline__ int nth_bit(int mask, int i) {
+  for (int k = 0; k < i && mask; ++k) mask &= mask - 1;
+  return mask & (-mask);
 }
 
+// Tile offset of rest index r for the tensor-core cross matrix.  A
+// half-warp's fragment loads cover window entries 0-3 (window bits 0-1)
+// times rest indices 2t (rest bits 1-2), so rest bits 1 and 2 take tile
+// bits whose bank residues (bit position mod 4: the swizzle folds tile bits
+// 4-7 and 8-11 onto 0-3) differ from each other and from those of window
+// bits 0-1; the other rest bits follow in ascending order.  The reduction
+// over rests does not depend on their order.  Needs at least three rest
+// bits (T >= 8 with 4-qubit windows).
 __device__ __forceinline__ int rest_offset(int r, int wmask, int rmask) {
-  int cov = low2_res(wmask), left = rmask, lead[2];
-  for (int i = 0; i < 2; ++i) {
-    int pick = pick_res(left, cov);
-    if (!pick) pick = left & (-left);
-    lead[i] = pick;   // zero when the rest has fewer bits
-    cov |= bank_res(pick);
-    left &= ~pick;
-  }
-  return ((r & 1) ? lead[0] : 0) | ((r & 2) ? lead[1] : 0) | deposit32(r >> 2, left);
+  const int cov = bank_res(nth_bit(wmask, 0)) | bank_res(nth_bit(wmask, 1));
+  int left = rmask;
+  const int b1 = pick_res(left, cov);
+  left &= ~b1;
+  const int b2 = pick_res(left, cov | bank_res(b1));
+  left &= ~b2;
+  const int b0 = left & (-left);
+  left &= ~b0;
+  return ((r & 1) ? b0 : 0) | ((r & 2) ? b1 : 0) | ((r & 4) ? b2 : 0) | deposit32(r >> 3, left);
 }
 
 // Tile offset of window position p for the tensor-core gate application.
-// Its loads put window bits 0-1 and position bits 0-1 on a half-warp, its
-// stores window bits 0-1 and position bits 1-2, so position bit 1 takes a
-// residue outside the window's, bit 0 a fourth one and bit 2 the residue of
-// bit 0 where the tile has one.
+// Its loads put window bits 1-2 and position bits 0-1 on a half-warp, its
+// stores window bits 0-1 and position bits 1-2; positions bits 0-2 take
+// residues distinct from those, where the tile has them.  Needs at least
+// three position bits.
 __device__ __forceinline__ int apply_pos_offset(int p, int wmask, int rmask) {
-  const int cov = low2_res(wmask);
+  const int r0 = bank_res(nth_bit(wmask, 0)), r1 = bank_res(nth_bit(wmask, 1)), r2 = bank_res(nth_bit(wmask, 2));
   int left = rmask;
-  int p1 = pick_res(left, cov);
-  if (!p1) p1 = left & (-left);
+  const int p1 = pick_res(left, r0 | r1 | r2);
   left &= ~p1;
-  int p0 = pick_res(left, cov | bank_res(p1));
-  if (!p0) p0 = left & (-left);
+  const int p0 = pick_res(left, r1 | r2 | bank_res(p1));
   left &= ~p0;
-  int p2 = pick_res(left, 15 & ~bank_res(p0));
-  if (!p2 || !p0) p2 = pick_res(left, cov | bank_res(p1));
-  if (!p2) p2 = left & (-left);
+  const int p2 = pick_res(left, r0 | r1 | bank_res(p1));
   left &= ~p2;
   return ((p & 1) ? p0 : 0) | ((p & 2) ? p1 : 0) | ((p & 4) ? p2 : 0) | deposit32(p >> 3, left);
 }
@@ -315,35 +315,35 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
   __syncthreads();
 }
 
-// ---- cross matrix on the tensor cores (4-qubit windows) -----------------------
+// ---- window products on the tensor cores (4-qubit windows) ---------------------
 //
-// M = conj(Z) X^T with Z, X the 16 x rest matrices of the tile, as real
-// m16n8k8 TF32 products (rows: window entry of z, columns: window entry of
-// x, reduction: rests):
-//   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T.
-// Each fp32 operand v is split v = hi + lo by Veltkamp's splitting
-// (multiply by 2^13 + 1): hi is v rounded to nearest with 11 significant
-// bits, the tf32 precision, and lo = v - hi is exact with at most 12
-// significant bits and |lo| <= 2^-11 |v|.  The tensor core ignores the low
-// 13 bits of a tf32 operand, so it reads hi exactly and lo truncated by at
-// most one bit.  A product is taken as lo_a hi_b + hi_a lo_b + hi_a hi_b
-// (the 3xTF32 scheme): the dropped lo_a lo_b and the truncation of lo leave
-// a relative error of at most 3 * 2^-22 per product.  The split runs on the
-// FP32 pipe (explicitly rounded operations, no contraction).
-// A warp owns k-steps of 8 rests; its fragments come straight from the
-// swizzled tile (no staging): lane (g, t) reads rows/columns g and g + 8 at
-// rests 8 s + t and 8 s + t + 4.  Accumulators, for the column tiles nt = 0
-// (entries 0..7) and 1 (8..15): acc[nt][0] = Zr Xr^T, acc[nt][1] = Zr Xi^T,
-// acc[nt][2] = Zi Xr^T, acc[nt][3] = Zi Xi^T (four independent chains).
-__device__ __forceinline__ void tf32_split(float v, unsigned& hi, unsigned& lo) {
-  const float g = __fmul_rn(v, 8193.f);
-  const float h = __fsub_rn(g, __fsub_rn(g, v));
-  hi = __float_as_uint(h);
-  lo = __float_as_uint(__fsub_rn(v, h));
+// The two products of a pass, the cross matrix M = conj(Z) X^T (rows: window
+// entry of z, columns: window entry of x, reduction over rests) and the
+// window gates V <- G V, run as real m16n8k16 FP16 products with FP32
+// accumulation:
+//   Re M = Zr Xr^T + Zi Xi^T,   Im M = Zr Xi^T - Zi Xr^T,
+//   Re V' = Gr Vr + (-Gi) Vi,   Im V' = Gr Vi + Gi Vr.
+// Each operand is scaled by an exact power of two and split v s = hi + lo,
+// hi = fp16(v s) and lo = fp16(v s - hi), both rounded to nearest (v s - hi
+// is exact in FP32); a product is lo_a hi_b + hi_a lo_b + hi_a hi_b.  With
+// 11-bit hi and lo the dropped lo_a lo_b and the rounding of lo leave a
+// relative error of about 3 * 2^-24 per product, as long as lo is a normal
+// FP16 number: the scale puts typical amplitudes near 16 and keeps every
+// |v s| <= 2^15 (below the FP16 maximum).  Fragments come straight from the
+// swizzled tile (no staging).
+__device__ __forceinline__ unsigned h2_bits(__half2 h) { return *reinterpret_cast<unsigned*>(&h); }
+
+// (a, b) = (element 2t, element 2t + 1) of an f16x2 fragment register
+__device__ __forceinline__ void f16_split2(float a, float b, float sc, unsigned& hi, unsigned& lo) {
+  const float as = a * sc, bs = b * sc;
+  const __half2 h = __floats2half2_rn(as, bs);
+  const float2 hf = __half22float2(h);
+  hi = h2_bits(h);
+  lo = h2_bits(__floats2half2_rn(as - hf.x, bs - hf.y));
 }
 
-__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
-  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+__device__ __forceinline__ void mma_f16(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
       "{%0,%1,%2,%3};\n"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
@@ -352,42 +352,61 @@ __device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], 
 // c += a b, the small products first
 __device__ __forceinline__ void mma3(float (&c)[4], const unsigned (&ah)[4], const unsigned (&al)[4],
                                      const unsigned (&bh)[2], const unsigned (&bl)[2]) {
-  mma_tf32(c, al, bh[0], bh[1]);
-  mma_tf32(c, ah, bl[0], bl[1]);
-  mma_tf32(c, ah, bh[0], bh[1]);
+  mma_f16(c, al, bh[0], bh[1]);
+  mma_f16(c, ah, bl[0], bl[1]);
+  mma_f16(c, ah, bh[0], bh[1]);
 }
 
-// Needs 2^(T - 4) >= 8 rests.
+// Scale of a state vector with 2^n amplitudes and norm `nrm`: 2^k with
+// 2^k nrm <= 2^min(n/2 + 4, 15), so |v s| <= 2^15 and typical amplitudes
+// (nrm 2^-n/2) land near 16.
+__device__ __forceinline__ float vec_scale(int n, double nrm) {
+  int e = 0;
+  frexp(nrm, &e);   // nrm < 2^e
+  const int top = n / 2 + 4 < 15 ? n / 2 + 4 : 15;
+  return ldexpf(1.f, top - e);
+}
+#define GATE_SCALE 256.f   // G entries (|g| <= 1) scaled into FP16's normal range
+
+// Cross matrix of one tile, accumulated into acc (scaled by sx sz).  A warp
+// owns k-steps of 16 rests; lane (g, t) reads window entries g and g + 8 at
+// rests 16 s + 2t, +1, +8, +9.  acc[nt][0..3] = Zr Xr^T, Zr Xi^T, Zi Xr^T,
+// Zi Xi^T for the column tiles nt = 0 (entries 0..7) and 1 (8..15).  Needs
+// 2^(T - 4) >= 16 rests.
 __device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2* xs, const float2* zs,
                                               float (&acc)[2][4][4]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const int w0 = sh.wl[gq], w1 = sh.wl[gq + 8];
-  const int nks = 1 << (sh.T - 7);
+  const float sx = sh.sx, sz = sh.sz;
+  const int nks = 1 << (sh.T - 8);
   for (int ks = warp; ks < nks; ks += nwarps) {
-    const int r0 = sh.rl[ks * 8 + tq], r1 = sh.rl[ks * 8 + tq + 4];
-    // A = Z: a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4)
-    const float2 z0 = zs[w0 ^ r0], z1 = zs[w1 ^ r0], z2 = zs[w0 ^ r1], z3 = zs[w1 ^ r1];
-    // B = X^T, column tile nt: b0 (rest t, entry 8 nt + g), b1 (rest t + 4, same entry)
-    const float2 x0 = xs[w0 ^ r0], x1 = xs[w0 ^ r1], x2 = xs[w1 ^ r0], x3 = xs[w1 ^ r1];
+    const int* rr = sh.rl + ks * 16 + 2 * tq;
+    const int r0 = rr[0], r1 = rr[1], r2 = rr[8], r3 = rr[9];
+    // A = Z: reg0 (g; 2t, 2t+1), reg1 (g+8; 2t, 2t+1), reg2 (g; 2t+8, 2t+9), reg3 (g+8; 2t+8, 2t+9)
+    const float2 za = zs[w0 ^ r0], zb = zs[w0 ^ r1], zc = zs[w1 ^ r0], zd = zs[w1 ^ r1];
+    const float2 ze = zs[w0 ^ r2], zf = zs[w0 ^ r3], zg = zs[w1 ^ r2], zh = zs[w1 ^ r3];
+    // B = X^T, column tile nt (entry 8 nt + g): reg0 (rests 2t, 2t+1), reg1 (2t+8, 2t+9)
+    const float2 xa = xs[w0 ^ r0], xb = xs[w0 ^ r1], xc = xs[w1 ^ r0], xd = xs[w1 ^ r1];
+    const float2 xe = xs[w0 ^ r2], xf = xs[w0 ^ r3], xg = xs[w1 ^ r2], xh = xs[w1 ^ r3];
     unsigned zrh[4], zrl[4], zih[4], zil[4];
-    tf32_split(z0.x, zrh[0], zrl[0]);
-    tf32_split(z1.x, zrh[1], zrl[1]);
-    tf32_split(z2.x, zrh[2], zrl[2]);
-    tf32_split(z3.x, zrh[3], zrl[3]);
-    tf32_split(z0.y, zih[0], zil[0]);
-    tf32_split(z1.y, zih[1], zil[1]);
-    tf32_split(z2.y, zih[2], zil[2]);
-    tf32_split(z3.y, zih[3], zil[3]);
+    f16_split2(za.x, zb.x, sz, zrh[0], zrl[0]);
+    f16_split2(zc.x, zd.x, sz, zrh[1], zrl[1]);
+    f16_split2(ze.x, zf.x, sz, zrh[2], zrl[2]);
+    f16_split2(zg.x, zh.x, sz, zrh[3], zrl[3]);
+    f16_split2(za.y, zb.y, sz, zih[0], zil[0]);
+    f16_split2(zc.y, zd.y, sz, zih[1], zil[1]);
+    f16_split2(ze.y, zf.y, sz, zih[2], zil[2]);
+    f16_split2(zg.y, zh.y, sz, zih[3], zil[3]);
     unsigned xrh[2][2], xrl[2][2], xih[2][2], xil[2][2];
-    tf32_split(x0.x, xrh[0][0], xrl[0][0]);
-    tf32_split(x1.x, xrh[0][1], xrl[0][1]);
-    tf32_split(x2.x, xrh[1][0], xrl[1][0]);
-    tf32_split(x3.x, xrh[1][1], xrl[1][1]);
-    tf32_split(x0.y, xih[0][0], xil[0][0]);
-    tf32_split(x1.y, xih[0][1], xil[0][1]);
-    tf32_split(x2.y, xih[1][0], xil[1][0]);
-    tf32_split(x3.y, xih[1][1], xil[1][1]);
+    f16_split2(xa.x, xb.x, sx, xrh[0][0], xrl[0][0]);
+    f16_split2(xe.x, xf.x, sx, xrh[0][1], xrl[0][1]);
+    f16_split2(xc.x, xd.x, sx, xrh[1][0], xrl[1][0]);
+    f16_split2(xg.x, xh.x, sx, xrh[1][1], xrl[1][1]);
+    f16_split2(xa.y, xb.y, sx, xih[0][0], xil[0][0]);
+    f16_split2(xe.y, xf.y, sx, xih[0][1], xil[0][1]);
+    f16_split2(xc.y, xd.y, sx, xih[1][0], xil[1][0]);
+    f16_split2(xg.y, xh.y, sx, xih[1][1], xil[1][1]);
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt) {
       mma3(acc[nt][0], zrh, zrl, xrh[nt], xrl[nt]);
@@ -400,70 +419,64 @@ __device__ __forceinline__ void pass_cross_tc(const PassShared& sh, const float2
 
 // V <- G V on the tensor cores, with V the 16 x position matrix of a tile
 // over a 4-qubit window (wlt: window entry -> tile offset, plt: position ->
-// tile offset) and G given as the A fragments `gf` of compose_gates:
-//   Re V' = Gr Vr + (-Gi) Vi,   Im V' = Gr Vi + Gi Vr
-// as 3xTF32 m16n8k8 products.  A warp owns column tiles of 8 positions; all
-// of its loads come before its stores and no other warp touches its
-// positions.  Needs 2^(T - 4) >= 8.
+// tile offset, sc: the vector's scale) and G given as the A fragments `gf`
+// of compose_gates (scaled by GATE_SCALE).  One k-step covers the 16 window
+// entries.  A warp owns column tiles of 8 positions; all of its loads come
+// before its stores and no other warp touches its positions.  Needs
+// 2^(T - 4) >= 8.
 static_assert(PASS_THREADS / 32 * 4 >= (1 << (GT - 7)), "four column tiles per warp cover a tile");
-__device__ __forceinline__ void tile_apply_tc(const int* wlt, const int* plt, const uint4 (*gf)[4][32], int T,
-                                              float2* v) {
+__device__ __forceinline__ void tile_apply_tc(const int* wlt, const int* plt, const uint4 (*gf)[32], int T,
+                                              float sc, float2* v) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const int nnt = 1 << (T - 7), npos = 1 << (T - 4);   // column tiles, positions of the tile
+  const uint4 frh = gf[0][lane], frl = gf[1][lane], fih = gf[2][lane], fil = gf[3][lane];
+  const uint4 fnh = gf[4][lane], fnl = gf[5][lane];
+  const unsigned grh[4] = {frh.x, frh.y, frh.z, frh.w}, grl[4] = {frl.x, frl.y, frl.z, frl.w};
+  const unsigned gih[4] = {fih.x, fih.y, fih.z, fih.w}, gil[4] = {fil.x, fil.y, fil.z, fil.w};
+  const unsigned gnh[4] = {fnh.x, fnh.y, fnh.z, fnh.w}, gnl[4] = {fnl.x, fnl.y, fnl.z, fnl.w};
+  // B rows (window entries) 2t, 2t+1, 2t+8, 2t+9
+  const int wa = wlt[2 * tq], wb = wlt[2 * tq + 1], wc = wlt[2 * tq + 8], wd = wlt[2 * tq + 9];
   float c[4][2][4];   // [column tile of this warp][Re, Im][fragment]
 #pragma unroll
   for (int e = 0; e < 32; ++e) (&c[0][0][0])[e] = 0.f;
+  // column tiles past the tile's positions (T < GT) read wrapped positions
+  // and are not stored
 #pragma unroll
-  for (int ks = 0; ks < 2; ++ks) {
-    const uint4 frh = gf[ks][0][lane], frl = gf[ks][1][lane];
-    const uint4 fih = gf[ks][2][lane], fil = gf[ks][3][lane];
-    const unsigned grh[4] = {frh.x, frh.y, frh.z, frh.w}, grl[4] = {frl.x, frl.y, frl.z, frl.w};
-    const unsigned gih[4] = {fih.x, fih.y, fih.z, fih.w}, gil[4] = {fil.x, fil.y, fil.z, fil.w};
-    unsigned ngih[4], ngil[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      ngih[i] = gih[i] ^ 0x80000000u;
-      ngil[i] = gil[i] ^ 0x80000000u;
-    }
-    const int wa = wlt[8 * ks + tq], wb = wlt[8 * ks + tq + 4];
-    // column tiles past the tile's positions (T < GT) read wrapped
-    // positions and are not stored
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int nt = warp + j * nwarps;
-      const int po = plt[(8 * nt + gq) & (npos - 1)];
-      // b0 = V[8 ks + t][8 nt + g], b1 = V[8 ks + t + 4][8 nt + g]
-      const float2 v0 = v[wa ^ po], v1 = v[wb ^ po];
-      unsigned rh[2], rl[2], ih[2], il[2];
-      tf32_split(v0.x, rh[0], rl[0]);
-      tf32_split(v1.x, rh[1], rl[1]);
-      tf32_split(v0.y, ih[0], il[0]);
-      tf32_split(v1.y, ih[1], il[1]);
-      mma3(c[j][0], grh, grl, rh, rl);
-      mma3(c[j][1], grh, grl, ih, il);
-      mma3(c[j][0], ngih, ngil, ih, il);
-      mma3(c[j][1], gih, gil, rh, rl);
-    }
+  for (int j = 0; j < 4; ++j) {
+    const int nt = warp + j * nwarps;
+    const int po = plt[(8 * nt + gq) & (npos - 1)];
+    const float2 va = v[wa ^ po], vb = v[wb ^ po], vc = v[wc ^ po], vd = v[wd ^ po];
+    unsigned rh[2], rl[2], ih[2], il[2];
+    f16_split2(va.x, vb.x, sc, rh[0], rl[0]);
+    f16_split2(vc.x, vd.x, sc, rh[1], rl[1]);
+    f16_split2(va.y, vb.y, sc, ih[0], il[0]);
+    f16_split2(vc.y, vd.y, sc, ih[1], il[1]);
+    mma3(c[j][0], grh, grl, rh, rl);
+    mma3(c[j][1], grh, grl, ih, il);
+    mma3(c[j][0], gnh, gnl, ih, il);
+    mma3(c[j][1], gih, gil, rh, rl);
   }
-  // c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1)
+  // c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1), scaled
+  // by sc GATE_SCALE (a power of two: the unscaling is exact)
+  const float us = 1.f / (sc * GATE_SCALE);
   const int w0 = wlt[gq], w1 = wlt[gq + 8];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int nt = warp + j * nwarps;
     if (nt >= nnt) continue;
     const int p0 = plt[8 * nt + 2 * tq], p1 = plt[8 * nt + 2 * tq + 1];
-    v[w0 ^ p0] = cf(c[j][0][0], c[j][1][0]);
-    v[w0 ^ p1] = cf(c[j][0][1], c[j][1][1]);
-    v[w1 ^ p0] = cf(c[j][0][2], c[j][1][2]);
-    v[w1 ^ p1] = cf(c[j][0][3], c[j][1][3]);
+    v[w0 ^ p0] = cf(c[j][0][0] * us, c[j][1][0] * us);
+    v[w0 ^ p1] = cf(c[j][0][1] * us, c[j][1][1] * us);
+    v[w1 ^ p0] = cf(c[j][0][2] * us, c[j][1][2] * us);
+    v[w1 ^ p1] = cf(c[j][0][3] * us, c[j][1][3] * us);
   }
 }
 
 // Previous group's peels on x and new gates on z (pass kernel).
 __device__ __forceinline__ void pass_apply_tc(const PassShared& sh, float2* xs, float2* zs) {
-  tile_apply_tc(sh.wlp, sh.plp, sh.gf[0], sh.T, xs);
-  tile_apply_tc(sh.wlp, sh.plp, sh.gf[1], sh.T, zs);
+  tile_apply_tc(sh.wlp, sh.plp, sh.gf[0], sh.T, sh.sx, xs);
+  tile_apply_tc(sh.wlp, sh.plp, sh.gf[1], sh.T, sh.sz, zs);
 }
 
 // The gate steps of one window: step s applies the row-major matrix gm[s]
@@ -476,11 +489,11 @@ struct GateList {
 
 // Compose up to two gate lists into 16 x 16 matrices G (threads 0-31:
 // matrix t / 16, column t % 16, written to `scratch` as [matrix][row][col])
-// and split G into the A fragments of tile_apply_tc (one thread per matrix,
-// k-step and lane).  `scratch` aliases the tile buffers; the block must call
-// this uniformly.
+// and split GATE_SCALE G into the A fragments of tile_apply_tc (one thread
+// per matrix and lane): Gr hi, Gr lo, Gi hi, Gi lo, -Gi hi, -Gi lo.
+// `scratch` aliases the tile buffers; the block must call this uniformly.
 __device__ __forceinline__ void compose_gates(const GateList (&gl)[2], int nmat, float2* scratch,
-                                              uint4 (*gf)[2][4][32]) {
+                                              uint4 (*gf)[6][32]) {
   const int t = threadIdx.x;
   if (t < 16 * nmat) {
     const int m = t >> 4, col = t & 15;
@@ -494,32 +507,33 @@ __device__ __forceinline__ void compose_gates(const GateList (&gl)[2], int nmat,
     for (int w = 0; w < 16; ++w) scratch[m * 256 + w * 16 + col] = a[w];
   }
   __syncthreads();
-  for (int e = t; e < nmat * 2 * 32; e += blockDim.x) {
-    const int m = e >> 6, ks = (e >> 5) & 1, lane = e & 31, gq = lane >> 2, tq = lane & 3;
-    // a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4) of the k-step
+  for (int e = t; e < nmat * 32; e += blockDim.x) {
+    const int m = e >> 5, lane = e & 31, gq = lane >> 2, tq = lane & 3;
+    // reg0 (g; 2t, 2t+1), reg1 (g+8; 2t, 2t+1), reg2 (g; 2t+8, 2t+9), reg3 (g+8; 2t+8, 2t+9)
     const float2* G = scratch + m * 256;
-    const float2 g0 = G[gq * 16 + 8 * ks + tq], g1 = G[(gq + 8) * 16 + 8 * ks + tq];
-    const float2 g2 = G[gq * 16 + 8 * ks + tq + 4], g3 = G[(gq + 8) * 16 + 8 * ks + tq + 4];
-    uint4 rh, rl, ih, il;
-    tf32_split(g0.x, rh.x, rl.x);
-    tf32_split(g1.x, rh.y, rl.y);
-    tf32_split(g2.x, rh.z, rl.z);
-    tf32_split(g3.x, rh.w, rl.w);
-    tf32_split(g0.y, ih.x, il.x);
-    tf32_split(g1.y, ih.y, il.y);
-    tf32_split(g2.y, ih.z, il.z);
-    tf32_split(g3.y, ih.w, il.w);
-    gf[m][ks][0][lane] = rh;
-    gf[m][ks][1][lane] = rl;
-    gf[m][ks][2][lane] = ih;
-    gf[m][ks][3][lane] = il;
+    const int rows[4] = {gq, gq + 8, gq, gq + 8}, cols[4] = {2 * tq, 2 * tq, 2 * tq + 8, 2 * tq + 8};
+    unsigned rh[4], rl[4], ih[4], il[4], nh[4], nl[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float2 a = G[rows[r] * 16 + cols[r]], b = G[rows[r] * 16 + cols[r] + 1];
+      f16_split2(a.x, b.x, GATE_SCALE, rh[r], rl[r]);
+      f16_split2(a.y, b.y, GATE_SCALE, ih[r], il[r]);
+      f16_split2(-a.y, -b.y, GATE_SCALE, nh[r], nl[r]);
+    }
+    gf[m][0][lane] = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+    gf[m][1][lane] = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+    gf[m][2][lane] = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+    gf[m][3][lane] = make_uint4(il[0], il[1], il[2], il[3]);
+    gf[m][4][lane] = make_uint4(nh[0], nh[1], nh[2], nh[3]);
+    gf[m][5][lane] = make_uint4(nl[0], nl[1], nl[2], nl[3]);
   }
   __syncthreads();
 }
 
-// Sum the warps' M (fixed order) into the chunk's partial.  `red` aliases
-// the tile buffers (needs nwarps * 256 double2).
-__device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][4][4], double2* red, double2* out) {
+// Sum the warps' M (fixed order) into the chunk's partial, unscaled by
+// 1 / (sx sz) (exact).  `red` aliases the tile buffers (needs
+// nwarps * 256 double2).
+__device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][4][4], double us, double2* red, double2* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   __syncthreads();   // tile buffers free
@@ -529,7 +543,7 @@ __device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][4][4], doubl
     for (int e = 0; e < 4; ++e) {
       const int i = gq + (e >> 1) * 8, k = nt * 8 + 2 * tq + (e & 1);
       red[warp * GMM + i * GM + k] =
-          cd((double)acc[nt][0][e] + (double)acc[nt][3][e], (double)acc[nt][1][e] - (double)acc[nt][2][e]);
+          cd(((double)acc[nt][0][e] + (double)acc[nt][3][e]) * us, ((double)acc[nt][1][e] - (double)acc[nt][2][e]) * us);
     }
   __syncthreads();
   for (int ent = threadIdx.x; ent < GMM; ent += blockDim.x) {
@@ -604,7 +618,7 @@ __device__ __forceinline__ void pass_store(const PassShared& sh, float2* xg, flo
 // read as a counter
 __device__ __forceinline__ int64_t next_in_mask(int64_t x, int64_t mask) { return ((x | ~mask) + 1) & mask; }
 
-// TC: the cross matrix on the tensor cores (U = 4, T >= 7).
+// TC: the window products on the tensor cores (U = 4, T >= 8).
 template <int U, bool TC>
 __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& gd, const PassShared& sh, float2* xs,
                                            float2* zs, int g, int b, int chunk, float2* psi, const float2* z_in,
@@ -641,7 +655,9 @@ __device__ __forceinline__ void pass_chunk(const BatchDev& bd, const GroupDev& g
     __syncthreads();
     base = next_in_mask(base, rest_mask);
   }
-  if constexpr (TC) pass_flush_tc(tacc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
+  if constexpr (TC)
+    pass_flush_tc(tacc, 1.0 / ((double)sh.sx * (double)sh.sz), reinterpret_cast<double2*>(xs),
+                  gd.partials + (int64_t)chunk * GMM);
   else pass_flush<U>(acc, reinterpret_cast<double2*>(xs), gd.partials + (int64_t)chunk * GMM);
 }
 
@@ -649,7 +665,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
                                                               const float2* z_in, float2* z_out,
                                                               const double2* gates, const double2* old_gates,
                                                               const signed char* arity, const int* nlayers,
-                                                              const int* active) {
+                                                              const int* active, const double2* znorm) {
   extern __shared__ __align__(16) unsigned char dyn[];
   float2* xs = reinterpret_cast<float2*>(dyn);
   float2* zs = xs + (1 << GT);
@@ -695,6 +711,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       sh.wml_c = wc;
       sh.wml_p = wp;   // the current window when g = 0
       sh.npk = g > 0 ? (prv.cnt < GMAXSTEPS ? prv.cnt : GMAXSTEPS) : 0;
+      sh.sx = vec_scale(n, 1.0);   // x = C|0> (or its peels) has unit norm
+      sh.sz = vec_scale(n, znorm ? sqrt(fabs(znorm[b].x)) : 1.0);
     }
     __syncthreads();
     const int full = (1 << T) - 1;
@@ -715,8 +733,8 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       sh.wlp[a] = swz(deposit32(a, sh.wml_p));
     }
     for (int r = threadIdx.x; r < (1 << (T - U)); r += blockDim.x) {
-      sh.rl[r] = swz(rest_offset(r, sh.wml_c, full & ~sh.wml_c));
-      sh.plp[r] = swz(U == 4 && T >= 7 ? apply_pos_offset(r, sh.wml_p, full & ~sh.wml_p)
+      sh.rl[r] = swz(U == 4 && T >= 8 ? rest_offset(r, sh.wml_c, full & ~sh.wml_c) : deposit32(r, full & ~sh.wml_c));
+      sh.plp[r] = swz(U == 4 && T >= 8 ? apply_pos_offset(r, sh.wml_p, full & ~sh.wml_p)
                                         : deposit32(r, full & ~sh.wml_p));
     }
     if (g > 0) {
@@ -738,11 +756,11 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_group_pass
       }
     }
     __syncthreads();
-    if (U == 4 && T >= 7 && g > 0) {
+    if (U == 4 && T >= 8 && g > 0) {
       const GateList gl[2] = {{sh.pk, sh.phi, sh.plo, sh.gm[0], sh.npk}, {sh.pk, sh.phi, sh.plo, sh.gm[1], sh.npk}};
       compose_gates(gl, 2, xs, sh.gf);
     }
-    if (U == 4 && T >= 7) pass_chunk<4, true>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
+    if (U == 4 && T >= 8) pass_chunk<4, true>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 4) pass_chunk<4, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else if (U == 3) pass_chunk<3, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
     else pass_chunk<2, false>(bd, gd, sh, xs, zs, g, b, chunk, psi, z_in, z_out);
@@ -765,7 +783,8 @@ struct RebuildShared {
   int pl[2][1 << (GT - GW)];       // position -> swizzled tile offset
   int d0[64], d1[64];
   float2 gm[2][GMAXSTEPS][16];     // the gates, row-major complex
-  uint4 gf[2][2][4][32];           // [window][k-step][Gr hi, Gr lo, Gi hi, Gi lo][lane]: tensor-core A fragments
+  uint4 gf[2][6][32];              // [window][Gr hi, Gr lo, Gi hi, Gi lo, -Gi hi, -Gi lo][lane]: A fragments
+  float sc;                        // tensor-core scale of the vector (a power of two)
 };
 
 template <int U>
@@ -783,7 +802,7 @@ __device__ __forceinline__ void rebuild_apply(const RebuildShared& sh, int w, fl
   }
 }
 
-// TC: the windows' gates on the tensor cores (U = 4, T >= 7).
+// TC: the windows' gates on the tensor cores (U = 4, T >= 8).
 template <int U, bool TC>
 __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev& gd, const RebuildShared& sh,
                                               float2* xs, int b, int chunk, float2* psi) {
@@ -810,7 +829,7 @@ __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev
     cp_async_wait<0>();
     __syncthreads();
     for (int w = 0; w < sh.nw; ++w) {
-      if constexpr (TC) tile_apply_tc(sh.wl[w], sh.pl[w], sh.gf[w], sh.T, xs);
+      if constexpr (TC) tile_apply_tc(sh.wl[w], sh.pl[w], sh.gf[w], sh.T, sh.sc, xs);
       else rebuild_apply<U>(sh, w, xs);
       __syncthreads();
     }
@@ -880,6 +899,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
       sh.pos_mask = pm;
       sh.T = T;
       sh.nw = nw;
+      sh.sc = vec_scale(n, 1.0);   // C|0> and the normalised working vector of the layer stage
     }
     __syncthreads();
     const int full = (1 << T) - 1;
@@ -900,7 +920,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
     }
     for (int t = threadIdx.x; t < 2 * (1 << (T - U)); t += blockDim.x) {
       const int w = t / (1 << (T - U)), r = t % (1 << (T - U));
-      sh.pl[w][r] = swz(U == 4 && T >= 7 && !exact ? apply_pos_offset(r, sh.wm[w], full & ~sh.wm[w])
+      sh.pl[w][r] = swz(U == 4 && T >= 8 && !exact ? apply_pos_offset(r, sh.wm[w], full & ~sh.wm[w])
                                          : deposit32(r, full & ~sh.wm[w]));
     }
     for (int t = threadIdx.x; t < 2 * GMAXSTEPS * 16; t += blockDim.x) {
@@ -917,7 +937,7 @@ __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pa
       sh.gm[w][st][e] = cf((float)v.x, (float)v.y);
     }
     __syncthreads();
-    if (U == 4 && T >= 7 && !exact) {
+    if (U == 4 && T >= 8 && !exact) {
       const GateList gl[2] = {{sh.pk[0], sh.phi[0], sh.plo[0], sh.gm[0], sh.nst[0]},
                               {sh.pk[1], sh.phi[1], sh.plo[1], sh.gm[1], sh.nst[1]}};
       compose_gates(gl, nw, xs, sh.gf);
@@ -1134,7 +1154,7 @@ void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float
 
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
                       const double2* gates, const signed char* arity, const int* nlayers, const int* active,
-                      cudaStream_t s) {
+                      const double2* znorm, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(k_group_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1146,7 +1166,7 @@ int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi
   if (grid < 1) grid = 1;
   qm_note_launch();
   k_group_pass<<<grid, PASS_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,
-                                                          nlayers, active);
+                                                          nlayers, active, znorm);
   return 0;
 }
 

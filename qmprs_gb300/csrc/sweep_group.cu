@@ -813,37 +813,47 @@ __device__ __forceinline__ void rebuild_chunk(const BatchDev& bd, const GroupDev
   float2* xv = psi + bd.vec_off[b];
   const int64_t t0 = (int64_t)gd.chunk_idx[chunk] * GCHUNK;
   const int64_t t1 = t0 + GCHUNK < ntiles ? t0 + GCHUNK : ntiles;
-  int64_t base = deposit_bits(t0, rest_mask);
   const int t = threadIdx.x, lo = sh.d0[t & 63], st = swz(t);
-  for (int64_t tt = t0; tt < t1; ++tt) {
-    const float2* xg = xv + base;
+  // double-buffered: tile tt + 1 streams into the other buffer while tile
+  // tt is processed (one commit group per tile)
+  auto issue = [&](int64_t gbase, float2* buf) {
+    const float2* xg = xv + gbase;
     if (sh.T == GT) {
 #pragma unroll
       for (int u = 0; u < PASS_PER; ++u)
-        cp_async8(xs + (st ^ swz(u * PASS_THREADS)), xg + (lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]));
+        cp_async8(buf + (st ^ swz(u * PASS_THREADS)), xg + (lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]));
     } else {
       for (int li = t; li < (1 << sh.T); li += blockDim.x)
-        cp_async8(xs + swz(li), xg + (sh.d0[li & 63] | sh.d1[li >> 6]));
+        cp_async8(buf + swz(li), xg + (sh.d0[li & 63] | sh.d1[li >> 6]));
     }
+  };
+  int64_t base = deposit_bits(t0, rest_mask);
+  issue(base, xs);
+  cp_async_commit();
+  for (int64_t tt = t0; tt < t1; ++tt) {
+    float2* cur = xs + (((tt - t0) & 1) << GT);
+    const int64_t nbase = next_in_mask(base, rest_mask);
+    if (tt + 1 < t1) issue(nbase, xs + ((((tt - t0) + 1) & 1) << GT));
     cp_async_commit();
-    cp_async_wait<0>();
+    cp_async_wait<1>();   // all but the newest group: tile tt has landed
     __syncthreads();
     for (int w = 0; w < sh.nw; ++w) {
-      if constexpr (TC) tile_apply_tc(sh.wl[w], sh.pl[w], sh.gf[w], sh.T, sh.sc, xs);
-      else rebuild_apply<U>(sh, w, xs);
+      if constexpr (TC) tile_apply_tc(sh.wl[w], sh.pl[w], sh.gf[w], sh.T, sh.sc, cur);
+      else rebuild_apply<U>(sh, w, cur);
       __syncthreads();
     }
     float2* xw = xv + base;
     if (sh.T == GT) {
 #pragma unroll
       for (int u = 0; u < PASS_PER; ++u)
-        xw[lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]] = xs[st ^ swz(u * PASS_THREADS)];
+        xw[lo | sh.d1[(t >> 6) + u * (PASS_THREADS / 64)]] = cur[st ^ swz(u * PASS_THREADS)];
     } else {
-      for (int li = t; li < (1 << sh.T); li += blockDim.x) xw[sh.d0[li & 63] | sh.d1[li >> 6]] = xs[swz(li)];
+      for (int li = t; li < (1 << sh.T); li += blockDim.x) xw[sh.d0[li & 63] | sh.d1[li >> 6]] = cur[swz(li)];
     }
-    __syncthreads();
-    base = next_in_mask(base, rest_mask);
+    __syncthreads();   // cur is read out before tile tt + 2 is issued into it
+    base = nbase;
   }
+  cp_async_wait<0>();
 }
 
 __global__ void __launch_bounds__(PASS_THREADS, PASS_BLOCKS_PER_SM) k_rebuild_pass(BatchDev bd, GroupDev gd,
@@ -1148,7 +1158,7 @@ void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float
   int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
   if (grid < 1) grid = 1;
   qm_note_launch();
-  k_rebuild_pass<<<grid, PASS_THREADS, (size_t)sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
+  k_rebuild_pass<<<grid, PASS_THREADS, (size_t)2 * sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
                                                                           nlayers, active, mode, layer, exact);
 }
 

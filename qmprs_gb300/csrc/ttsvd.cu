@@ -23,7 +23,7 @@
 #include "device_common.cuh"
 
 #define TT_CH 32
-#define TT_EIG_SMEM_W 64   // widest Gram diagonalised in shared memory (2 x 64 KB)
+#define TT_EIG_SMEM_W 64   // widest Gram diagonalised in shared memory (3 x 65 KB)
 
 __host__ __device__ inline int chi_eff(int chi, int n) {
   const int cap = 1 << (n / 2);
@@ -169,18 +169,145 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
   }
 }
 
+// ---- Jacobi rounds in either precision -----------------------------------------
+
+__device__ __forceinline__ float2 jmk(float re, float im) { return cf(re, im); }
+__device__ __forceinline__ double2 jmk(double re, double im) { return cd(re, im); }
+template <class C, class R>
+__device__ __forceinline__ C jscale(C a, R t) { return jmk(a.x * t, a.y * t); }
+template <class C>
+__device__ __forceinline__ C jmul(C a, C b) { return jmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <class C>
+__device__ __forceinline__ C jadd(C a, C b) { return jmk(a.x + b.x, a.y + b.y); }
+template <class C>
+__device__ __forceinline__ C jsub(C a, C b) { return jmk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float jsqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double jsqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float jabs(float2 a) { return hypotf(a.x, a.y); }
+__device__ __forceinline__ double jabs(double2 a) { return hypot(a.x, a.y); }
+
+template <class C, class R>
+struct JacobiShared {
+  R c[TT_MAXW / 2];
+  C se[TT_MAXW / 2], sce[TT_MAXW / 2];
+  int p[TT_MAXW / 2], q[TT_MAXW / 2], flag[TT_MAXW / 2];
+  int rot;
+};
+
+// Parallel cyclic Jacobi (round-robin pairing, w / 2 disjoint rotations per
+// round) on the Hermitian G (row-major, stride ld), accumulating V <- V R.
+// A pair rotates unless |g_pq| <= rel sqrt(|g_pp g_qq|) or |g_pq| <=
+// floor_abs.  Runs whole sweeps until one makes no rotation (at most
+// max_sweeps).  The block must call it uniformly.
+template <class C, class R>
+__device__ void jacobi_run(C* G, C* V, int w, int ld, R rel, R floor_abs, int max_sweeps, JacobiShared<C, R>& js) {
+  const int half = w / 2;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) js.rot = 0;
+    __syncthreads();
+    for (int k = 0; k < w - 1; ++k) {
+      if (threadIdx.x < half) {
+        const int i = threadIdx.x;
+        const int t1 = i, t2 = w - 1 - i;
+        int p = t1 == 0 ? 0 : 1 + ((t1 - 1 + k) % (w - 1));
+        int q = 1 + ((t2 - 1 + k) % (w - 1));
+        if (p > q) {
+          const int tmp = p;
+          p = q;
+          q = tmp;
+        }
+        const C g = G[p * ld + q];
+        const R ag = jabs(g);
+        const R app = G[p * ld + p].x, aqq = G[q * ld + q].x;
+        const int rot = !(ag == R(0) || ag <= rel * jsqrt(fabs(app * aqq)) || ag <= floor_abs);
+        js.p[i] = p;
+        js.q[i] = q;
+        js.flag[i] = rot;
+        if (rot) {
+          const R zeta = (aqq - app) / (R(2) * ag);
+          const R t = (zeta >= R(0) ? R(1) : R(-1)) / (fabs(zeta) + jsqrt(R(1) + zeta * zeta));
+          const R cc = R(1) / jsqrt(R(1) + t * t);
+          const R ss = cc * t;
+          const C e = jscale(g, R(1) / ag);
+          js.c[i] = cc;
+          js.se[i] = jscale(e, ss);
+          js.sce[i] = jscale(jmk(e.x, -e.y), ss);
+          js.rot = 1;
+        }
+      }
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
+        const int i = idx / w, row = idx % w;
+        if (!js.flag[i]) continue;
+        const int p = js.p[i], q = js.q[i];
+        const R cc = js.c[i];
+        const C se = js.se[i], sce = js.sce[i];
+        const C xp = G[row * ld + p], xq = G[row * ld + q];
+        G[row * ld + p] = jsub(jscale(xp, cc), jmul(sce, xq));
+        G[row * ld + q] = jadd(jmul(se, xp), jscale(xq, cc));
+        const C vp = V[row * ld + p], vq = V[row * ld + q];
+        V[row * ld + p] = jsub(jscale(vp, cc), jmul(sce, vq));
+        V[row * ld + q] = jadd(jmul(se, vp), jscale(vq, cc));
+      }
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
+        const int i = idx / w, col = idx % w;
+        if (!js.flag[i]) continue;
+        const int p = js.p[i], q = js.q[i];
+        const R cc = js.c[i];
+        const C se = js.se[i], sce = js.sce[i];
+        const C xp = G[p * ld + col], xq = G[q * ld + col];
+        G[p * ld + col] = jsub(jscale(xp, cc), jmul(se, xq));
+        G[q * ld + col] = jadd(jmul(sce, xp), jscale(xq, cc));
+      }
+      __syncthreads();
+      if (threadIdx.x < half && js.flag[threadIdx.x]) {
+        const int p = js.p[threadIdx.x], q = js.q[threadIdx.x];
+        G[p * ld + q] = jmk(R(0), R(0));
+        G[q * ld + p] = jmk(R(0), R(0));
+        G[p * ld + p].y = R(0);
+        G[q * ld + q].y = R(0);
+      }
+      __syncthreads();
+    }
+    if (!js.rot) break;
+    __syncthreads();
+  }
+}
+
+// C = A^H B (adj = true) or A B, w x w row-major matrices of stride ld in
+// shared memory; C is neither A nor B.
+__device__ void smem_matmul(const double2* A, const double2* B, double2* Cm, int w, int ld, bool adj) {
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    const int i = e / w, j = e % w;
+    double2 acc = czero();
+    if (adj)
+      for (int k = 0; k < w; ++k) acc = cadd(acc, cmulc(A[k * ld + i], B[k * ld + j]));
+    else
+      for (int k = 0; k < w; ++k) acc = cadd(acc, cmul(A[i * ld + k], B[k * ld + j]));
+    Cm[i * ld + j] = acc;
+  }
+}
+
 // One CTA per state; G and V are row-major w x w.  For w <= TT_EIG_SMEM_W
 // they live in shared memory (copied from `gram`, written back to `gram`
 // and `vwork` at the end), otherwise in place in global memory: each
 // Jacobi round is four block-wide phases, and shared memory takes the
 // memory latency out of them.
+//
+// In shared memory the eigenvectors are found in two precisions.  FP32
+// Jacobi sweeps on a float copy of G converge V to FP32 accuracy at the
+// FP32 rate; V is then made orthonormal in FP64 by one Newton-Schulz step
+// V <- V (3I - V^H V) / 2 (its FP32 error of about 1e-7 leaves about 1e-14),
+// G is replaced by the similar, nearly diagonal V^H G V, and the FP64
+// Jacobi sweeps finish from there, accumulating into the same V.  On the
+// Grams of the benchmark family this cuts the FP64 rotations from about 8.4
+// sweeps' worth to about 2.2 (w = 64).
 __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step, int* bonds, double2* gram,
                                                           double2* vwork, int max_bond, double cutoff,
                                                           double2* vsel, double2* tensors, int chi) {
-  __shared__ double s_c[TT_MAXW / 2];
-  __shared__ double2 s_se[TT_MAXW / 2], s_sce[TT_MAXW / 2];
-  __shared__ int s_p[TT_MAXW / 2], s_q[TT_MAXW / 2], s_flag[TT_MAXW / 2];
-  __shared__ int s_rot;
+  __shared__ JacobiShared<double2, double> js64;
+  __shared__ JacobiShared<float2, float> js32;
   __shared__ double s_floor;
   __shared__ double s_lam[TT_MAXW];
   __shared__ int s_perm[TT_MAXW];
@@ -206,11 +333,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   const int ld = in_smem ? w + 1 : w;   // padded rows: column walks hit distinct banks
   double2* G = in_smem ? eig_sm : Gg;
   double2* V = in_smem ? eig_sm + w * ld : Vg;
+  double2* Sc = eig_sm + 2 * w * ld;    // scratch (shared memory path only)
   if (in_smem)
     for (int e = threadIdx.x; e < w * w; e += blockDim.x) G[(e / w) * ld + e % w] = Gg[e];
-  for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   __syncthreads();
-  const int half = w / 2;
   // Absolute rotation floor: off-diagonals at most 1e-15 of the trace move
   // no eigenvalue by more than that (five orders below the 1e-10
   // truncation cutoff).  Without it the rounding-level null-space block of
@@ -218,77 +344,62 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   if (threadIdx.x == 0) {
     double tr = 0.0;
     for (int i = 0; i < w; ++i) tr += fabs(G[i * ld + i].x);
-    s_floor = 1e-15 * tr;
+    s_floor = tr;
   }
   __syncthreads();
-  const double floor_abs = s_floor;
-  for (int sweep = 0; sweep < 40; ++sweep) {
-    if (threadIdx.x == 0) s_rot = 0;
-    __syncthreads();
-    for (int k = 0; k < w - 1; ++k) {
-      if (threadIdx.x < half) {
-        const int i = threadIdx.x;
-        const int t1 = i, t2 = w - 1 - i;
-        int p = t1 == 0 ? 0 : 1 + ((t1 - 1 + k) % (w - 1));
-        int q = 1 + ((t2 - 1 + k) % (w - 1));
-        if (p > q) { const int tmp = p; p = q; q = tmp; }
-        const double2 g = G[p * ld + q];
-        const double ag = cabs_(g);
-        const double app = G[p * ld + p].x, aqq = G[q * ld + q].x;
-        const int rot = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)) || ag <= floor_abs);
-        s_p[i] = p;
-        s_q[i] = q;
-        s_flag[i] = rot;
-        if (rot) {
-          const double zeta = (aqq - app) / (2.0 * ag);
-          const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          const double cc = 1.0 / sqrt(1.0 + t * t);
-          const double ss = cc * t;
-          const double2 e = cscale(g, 1.0 / ag);
-          s_c[i] = cc;
-          s_se[i] = cscale(e, ss);
-          s_sce[i] = cscale(cconj(e), ss);
-          s_rot = 1;
-        }
-      }
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
-        const int i = idx / w, row = idx % w;
-        if (!s_flag[i]) continue;
-        const int p = s_p[i], q = s_q[i];
-        const double cc = s_c[i];
-        const double2 se = s_se[i], sce = s_sce[i];
-        const double2 xp = G[row * ld + p], xq = G[row * ld + q];
-        G[row * ld + p] = csub(cscale(xp, cc), cmul(sce, xq));
-        G[row * ld + q] = cadd(cmul(se, xp), cscale(xq, cc));
-        const double2 vp = V[row * ld + p], vq = V[row * ld + q];
-        V[row * ld + p] = csub(cscale(vp, cc), cmul(sce, vq));
-        V[row * ld + q] = cadd(cmul(se, vp), cscale(vq, cc));
-      }
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < half * w; idx += blockDim.x) {
-        const int i = idx / w, col = idx % w;
-        if (!s_flag[i]) continue;
-        const int p = s_p[i], q = s_q[i];
-        const double cc = s_c[i];
-        const double2 se = s_se[i], sce = s_sce[i];
-        const double2 xp = G[p * ld + col], xq = G[q * ld + col];
-        G[p * ld + col] = csub(cscale(xp, cc), cmul(se, xq));
-        G[q * ld + col] = cadd(cmul(sce, xp), cscale(xq, cc));
-      }
-      __syncthreads();
-      if (threadIdx.x < half && s_flag[threadIdx.x]) {
-        const int p = s_p[threadIdx.x], q = s_q[threadIdx.x];
-        G[p * ld + q] = czero();
-        G[q * ld + p] = czero();
-        G[p * ld + p].y = 0.0;
-        G[q * ld + q].y = 0.0;
-      }
-      __syncthreads();
+  const double tr = s_floor;
+  if (in_smem) {
+    float2* G32 = reinterpret_cast<float2*>(Sc);
+    float2* V32 = G32 + w * ld;
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int i = e / w, j = e % w;
+      const double2 g = G[i * ld + j];
+      G32[i * ld + j] = cf((float)g.x, (float)g.y);
+      V32[i * ld + j] = cf(i == j ? 1.f : 0.f, 0.f);
     }
-    if (!s_rot) break;
     __syncthreads();
+    jacobi_run<float2, float>(G32, V32, w, ld, 1e-7f, (float)(1e-7 * tr), 40, js32);
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int i = e / w, j = e % w;
+      V[i * ld + j] = f2d(V32[i * ld + j]);
+    }
+    __syncthreads();
+    // Newton-Schulz: Sc = (3I - V^H V) / 2, then V <- V Sc row by row (a
+    // warp per row, each lane two columns, written after the warp's reads)
+    smem_matmul(V, V, Sc, w, ld, true);
+    __syncthreads();
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int i = e / w, j = e % w;
+      const double2 v = Sc[i * ld + j];
+      Sc[i * ld + j] = cd((i == j ? 1.5 : 0.0) - 0.5 * v.x, -0.5 * v.y);
+    }
+    __syncthreads();
+    {
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+      for (int row = warp; row < w; row += nwarps) {
+        double2 o0 = czero(), o1 = czero();
+        for (int k = 0; k < w; ++k) {
+          const double2 v = V[row * ld + k];
+          if (lane < w) o0 = cadd(o0, cmul(v, Sc[k * ld + lane]));
+          if (lane + 32 < w) o1 = cadd(o1, cmul(v, Sc[k * ld + lane + 32]));
+        }
+        __syncwarp();
+        if (lane < w) V[row * ld + lane] = o0;
+        if (lane + 32 < w) V[row * ld + lane + 32] = o1;
+      }
+    }
+    __syncthreads();
+    // G <- V^H (G V)
+    smem_matmul(G, V, Sc, w, ld, false);
+    __syncthreads();
+    smem_matmul(V, Sc, G, w, ld, true);
+    __syncthreads();
+    for (int i = threadIdx.x; i < w; i += blockDim.x) G[i * ld + i].y = 0.0;
+  } else {
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   }
+  __syncthreads();
+  jacobi_run<double2, double>(G, V, w, ld, 1e-15, 1e-15 * tr, 40, js64);
   if (threadIdx.x == 0) {
     for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * ld + i].x; }
     for (int i = 1; i < w; ++i) {
@@ -425,7 +536,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_mps_contract(BatchDev bd, int
   }
 }
 
-#define TT_EIG_SMEM ((size_t)2 * TT_EIG_SMEM_W * (TT_EIG_SMEM_W + 1) * sizeof(double2))
+#define TT_EIG_SMEM ((size_t)3 * TT_EIG_SMEM_W * (TT_EIG_SMEM_W + 1) * sizeof(double2))   // G, V, scratch
 
 static int grid_for(const BatchDev& bd) {
   int g = bd.ntiles;

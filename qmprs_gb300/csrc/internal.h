@@ -102,7 +102,7 @@ struct GateSel {
 #define GM (1 << GW)
 #define GMM (GM * GM)
 #define GT 11
-#define GCHUNK 16
+#define GCHUNK 32
 #define GMAXSTEPS 8
 
 struct GroupEnt {

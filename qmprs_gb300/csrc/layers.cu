@@ -55,6 +55,14 @@ __device__ __forceinline__ void gram_rows(const float2* m, int64_t lo, int64_t h
   }
 }
 
+// Tiles of a state that take part in the Gram of a 2^c-row remainder: at
+// least 4096 rows (16 per thread) each, so a short remainder is not spread
+// over every tile of the state, each paying a full fp64 warp reduction.
+__device__ __forceinline__ int layer_gram_tiles(int c, int nt) {
+  const int64_t want = ((((int64_t)1) << c) + 4095) >> 12;
+  return want < nt ? (int)want : nt;
+}
+
 __global__ void __launch_bounds__(BLOCK_THREADS) k_layer_gram(BatchDev bd, int step, const float2* work,
                                                               const float2* src, const int* bonds,
                                                               double2* partials, const int* active) {
@@ -68,8 +76,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_layer_gram(BatchDev bd, int s
     const int r = bond[c + 1];
     if (r != 1 && r != 2) continue;
     const float2* m = (step == 0 ? work : src) + bd.vec_off[b];
+    const int vnt = layer_gram_tiles(c, nt);
+    if (bd.tile_idx[tile] >= vnt) continue;
     int64_t lo, hi;
-    tile_range(ipow2(c), bd.tile_idx[tile], nt, &lo, &hi);
+    tile_range(ipow2(c), bd.tile_idx[tile], vnt, &lo, &hi);
     double acc[32];
 #pragma unroll
     for (int e = 0; e < 32; ++e) acc[e] = 0.0;
@@ -95,7 +105,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_layer_eig(BatchDev bd, int st
     const int r = bond[c + 1];
     if (r != 1 && r != 2) continue;
     const int w = 2 * r;
-    const int np = bd.state_ntiles[b] * WARPS;
+    const int np = layer_gram_tiles(c, bd.state_ntiles[b]) * WARPS;   // the state's first tiles
     const int64_t p0 = (int64_t)bd.state_tile0[b] * WARPS;
     const int entry = threadIdx.x >> 4, lane = threadIdx.x & 15;
     double2 s = czero();

@@ -399,7 +399,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
-  jacobi_run<double2, double>(G, V, w, ld, 1e-15, 1e-15 * tr, 40, js64);
+  // After the FP32 stage the FP64 sweeps stop at 1e-13 of the trace (three
+  // orders below the 1e-10 cutoff; eigenvalues move by about 1e-15 of the
+  // trace against 1e-15): the remaining rotations are the null-space
+  // cluster's rounding noise.
+  jacobi_run<double2, double>(G, V, w, ld, 1e-15, (in_smem ? 1e-13 : 1e-15) * tr, 40, js64);
   if (threadIdx.x == 0) {
     for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * ld + i].x; }
     for (int i = 1; i < w; ++i) {

@@ -3,6 +3,8 @@
 // compare the exact routines the kernels run against the FP64 oracle.
 #include "small_linalg.h"
 
+#include "tile_layout.h"
+
 extern "C" {
 
 void hc_herm_eig(const double* g, int n, double* v_out, double* lam_out) {
@@ -63,5 +65,9 @@ void hc_ran_gate(int kind, const double* data, double* g_out) {
   const int m = kind <= 1 ? 4 : 2;
   for (int i = 0; i < m * m; ++i) { g_out[2 * i] = g[i].x; g_out[2 * i + 1] = g[i].y; }
 }
+
+int hc_swz(int li) { return swz(li); }
+int hc_rest_offset(int r, int wmask, int rmask) { return rest_offset(r, wmask, rmask); }
+int hc_apply_pos_offset(int p, int wmask, int rmask) { return apply_pos_offset(p, wmask, rmask); }
 
 }  // extern "C"

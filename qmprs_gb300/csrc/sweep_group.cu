@@ -32,6 +32,7 @@
 // vectors are not needed: the sweep's fidelity is the last step's trace.
 #include <cuda_fp16.h>
 
+#include "tile_layout.h"
 #include "window.cuh"
 
 // Gate of state b at backward step j: generated layer j / n, site
@@ -86,13 +87,6 @@ __device__ __forceinline__ int64_t deposit_bits(int64_t v, int64_t mask) {
   }
   return r;
 }
-
-// Shared-memory swizzle of a tile index: the low four bits (the float2
-// slot within a 128-byte bank row) are XORed with bits 4-7 and 8-11, so
-// that warps walking low, middle or high tile bits hit distinct banks.  The
-// map is linear over XOR, so for disjoint bit sets swz(a | b) =
-// swz(a) ^ swz(b) and the offset tables below hold swizzled values.
-__device__ __forceinline__ int swz(int li) { return li ^ (((li >> 4) ^ (li >> 8)) & 15); }
 
 // ---- group plan --------------------------------------------------------------
 
@@ -166,72 +160,6 @@ struct PassShared {
 
 // tile-local bit of global position p (p must be in pos_mask)
 __device__ __forceinline__ int tile_bit(int pos_mask, int p) { return __popc(pos_mask & ((1 << p) - 1)); }
-
-__device__ __forceinline__ int deposit32(int v, int mask) {
-  int r = 0;
-  while (mask) {
-    const int bit = mask & (-mask);
-    if (v & 1) r |= bit;
-    v >>= 1;
-    mask ^= bit;
-  }
-  return r;
-}
-
-// bank residue (one-hot) of a single-bit mask; 0 for no bit
-__device__ __forceinline__ int bank_res(int bit) { return bit ? 1 << ((__ffs(bit) - 1) & 3) : 0; }
-
-// lowest bit of `left` whose residue is not in `avoid`, else the lowest bit
-__device__ __forceinline__ int pick_res(int left, int avoid) {
-  for (int m = left; m; m &= m - 1) {
-    const int bit = __ffs(m) - 1;
-    if (!((avoid >> (bit & 3)) & 1)) return 1 << bit;
-  }
-  return left & (-left);
-}
-
-// the i-th lowest set bit of a mask (0 when it has fewer bits)
-__device__ __forceinline__ int nth_bit(int mask, int i) {
-  for (int k = 0; k < i && mask; ++k) mask &= mask - 1;
-  return mask & (-mask);
-}
-
-// Tile offset of rest index r for the tensor-core cross matrix.  A
-// half-warp's fragment loads cover window entries 0-3 (window bits 0-1)
-// times rest indices 2t (rest bits 1-2), so rest bits 1 and 2 take tile
-// bits whose bank residues (bit position mod 4: the swizzle folds tile bits
-// 4-7 and 8-11 onto 0-3) differ from each other and from those of window
-// bits 0-1; the other rest bits follow in ascending order.  The reduction
-// over rests does not depend on their order.  Needs at least three rest
-// bits (T >= 8 with 4-qubit windows).
-__device__ __forceinline__ int rest_offset(int r, int wmask, int rmask) {
-  const int cov = bank_res(nth_bit(wmask, 0)) | bank_res(nth_bit(wmask, 1));
-  int left = rmask;
-  const int b1 = pick_res(left, cov);
-  left &= ~b1;
-  const int b2 = pick_res(left, cov | bank_res(b1));
-  left &= ~b2;
-  const int b0 = left & (-left);
-  left &= ~b0;
-  return ((r & 1) ? b0 : 0) | ((r & 2) ? b1 : 0) | ((r & 4) ? b2 : 0) | deposit32(r >> 3, left);
-}
-
-// Tile offset of window position p for the tensor-core gate application.
-// Its loads put window bits 1-2 and position bits 0-1 on a half-warp, its
-// stores window bits 0-1 and position bits 1-2; positions bits 0-2 take
-// residues distinct from those, where the tile has them.  Needs at least
-// three position bits.
-__device__ __forceinline__ int apply_pos_offset(int p, int wmask, int rmask) {
-  const int r0 = bank_res(nth_bit(wmask, 0)), r1 = bank_res(nth_bit(wmask, 1)), r2 = bank_res(nth_bit(wmask, 2));
-  int left = rmask;
-  const int p1 = pick_res(left, r0 | r1 | r2);
-  left &= ~p1;
-  const int p0 = pick_res(left, r1 | r2 | bank_res(p1));
-  left &= ~p0;
-  const int p2 = pick_res(left, r0 | r1 | bank_res(p1));
-  left &= ~p2;
-  return ((p & 1) ? p0 : 0) | ((p & 2) ? p1 : 0) | ((p & 4) ? p2 : 0) | deposit32(p >> 3, left);
-}
 
 // Previous group's peels on x and new gates on z, over the previous
 // window: a thread owns the 2^U amplitudes of one window position and

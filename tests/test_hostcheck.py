@@ -195,3 +195,106 @@ def test_ran_gates_match_oracle(hc, seed):
     v = _c([0.6, 0.8j])
     hc.hc_ran_gate(3, _p(v), _p(o2))
     assert np.allclose(o2, D.last_site_unitary(v.reshape(1, 2, 1), 3, 3, "canonical"), atol=1e-13)
+
+
+# ---- tile layout of the pass kernels (qmprs_gb300/csrc/tile_layout.h) -------------
+
+def _layout(hc):
+    for f in (hc.hc_swz, hc.hc_rest_offset, hc.hc_apply_pos_offset):
+        f.restype = ctypes.c_int
+    return hc
+
+
+def _masks(T, u=4):
+    from itertools import combinations
+    for bits in combinations(range(T), u):
+        yield sum(1 << b for b in bits)
+
+
+def test_swizzle_is_a_linear_bijection(hc):
+    hc = _layout(hc)
+    vals = [hc.hc_swz(i) for i in range(1 << 12)]
+    assert sorted(vals) == list(range(1 << 12))
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        a, b = (int(x) for x in rng.integers(0, 1 << 12, 2))
+        assert hc.hc_swz(a ^ b) == vals[a] ^ vals[b]
+
+
+@pytest.mark.parametrize("T", [8, 9, 10, 11])
+def test_rest_and_position_orders_are_bijections(hc, T):
+    """Every 4-qubit window placement in a 2^T tile: the rest index and the
+    window position map one to one onto the tile bits outside the window
+    (a non-bijective order would drop rests from the cross matrix)."""
+    hc = _layout(hc)
+    full = (1 << T) - 1
+    for wmask in _masks(T):
+        rmask = full & ~wmask
+        subsets = set()
+        for r in range(1 << (T - 4)):
+            o = hc.hc_rest_offset(r, wmask, rmask)
+            assert o & ~rmask == 0
+            subsets.add(o)
+        assert len(subsets) == 1 << (T - 4)
+        pos = {hc.hc_apply_pos_offset(p, wmask, rmask) for p in range(1 << (T - 4))}
+        assert len(pos) == 1 << (T - 4) and all(o & ~rmask == 0 for o in pos)
+
+
+def _banks(addrs):
+    return len({hc_addr & 15 for hc_addr in addrs})
+
+
+def test_fragment_loads_hit_distinct_banks(hc):
+    """The cross matrix's fragment loads: a half-warp (window entries g = 0..3
+    times rest indices 2t, t = 0..3) reads 16 float2 slots; with the window
+    on four consecutive tile bits (the common case) they fall on 16 distinct
+    128-byte-row slots, and for every placement on at least 8."""
+    hc = _layout(hc)
+    T = 11
+    full = (1 << T) - 1
+    worst = 16
+    for wmask in _masks(T):
+        rmask = full & ~wmask
+        from_w = lambda a: hc.hc_swz(_deposit(a, wmask))
+        for e in (0, 1, 8, 9):
+            addrs = [from_w(g) ^ hc.hc_swz(hc.hc_rest_offset(2 * t + e, wmask, rmask)) for g in range(4)
+                     for t in range(4)]
+            worst = min(worst, _banks(addrs))
+            if wmask in (0b1111 << s for s in range(T - 3)):
+                assert _banks(addrs) == 16, (bin(wmask), e)
+    assert worst >= 8
+
+
+def _deposit(v, mask):
+    r, bit = 0, 0
+    while mask:
+        low = mask & -mask
+        if (v >> bit) & 1:
+            r |= low
+        bit += 1
+        mask ^= low
+    return r
+
+
+def test_gate_application_loads_and_stores_hit_distinct_banks(hc):
+    """The window-gate products: a half-warp loads entries 2t + e (t = 0..3)
+    at positions g (g = 0..3) and stores entries g at positions 2t + e; with
+    the window on four consecutive tile bits both are conflict-free, and for
+    every placement at most two-way."""
+    hc = _layout(hc)
+    T = 11
+    full = (1 << T) - 1
+    worst = 16
+    for wmask in _masks(T):
+        rmask = full & ~wmask
+        ent = lambda a: hc.hc_swz(_deposit(a, wmask))
+        pos = lambda p: hc.hc_swz(hc.hc_apply_pos_offset(p, wmask, rmask))
+        consecutive = wmask in (0b1111 << s for s in range(T - 3))
+        for e in (0, 1, 8, 9):
+            loads = [ent(2 * t + e) ^ pos(g) for g in range(4) for t in range(4)]
+            stores = [ent(g + (e & 8)) ^ pos(2 * t + (e & 1)) for g in range(4) for t in range(4)]
+            for addrs in (loads, stores):
+                worst = min(worst, _banks(addrs))
+                if consecutive:
+                    assert _banks(addrs) == 16, (bin(wmask), e)
+    assert worst >= 8

@@ -611,7 +611,9 @@ int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, do
     // six gates per read and write of the working state)
     launch_layer_plan(p->bd, p->gd, ar, ORDER_LAYER_INV, l, p->active, s);
     for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
-      launch_rebuild_pass(p->bd, p->gd, r, work, gates, ar, nullptr, p->active, s, ORDER_LAYER_INV, l);
+      // exact FP32 products: the next layer's bond-2 truncation decides at
+      // singular values near the 1e-10 cutoff of this working state
+      launch_rebuild_pass(p->bd, p->gd, r, work, gates, ar, nullptr, p->active, s, ORDER_LAYER_INV, l, true);
     launch_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
     launch_count_active(p->B, p->active, p->num_active, s);
     int na = 0;

@@ -20,9 +20,10 @@
 // A group therefore costs one pass over the vectors and one small kernel:
 //   k_group_pass   shared-memory tiles of 2^GT amplitudes: apply the
 //                  previous group's peels to x and its new gates to z,
-//                  write both back, and reduce this group's M (fp32 per
-//                  thread over a chunk of GCHUNK tiles, fp64 across the
-//                  block, one partial per chunk)
+//                  write both back, and reduce this group's M (both
+//                  products on the tensor cores, fp32 per warp over a
+//                  chunk of GCHUNK tiles, fp64 across the block, one
+//                  partial per chunk)
 //   k_group_polar  one block per state: sum the chunk partials in chunk
 //                  order, then run the group's steps on M in fp64 (target
 //                  update, peel, partial trace, polar factor), keeping the

@@ -69,5 +69,6 @@ void hc_ran_gate(int kind, const double* data, double* g_out) {
 int hc_swz(int li) { return swz(li); }
 int hc_rest_offset(int r, int wmask, int rmask) { return rest_offset(r, wmask, rmask); }
 int hc_apply_pos_offset(int p, int wmask, int rmask) { return apply_pos_offset(p, wmask, rmask); }
+float hc_vec_scale(int n, double nrm) { return vec_scale(n, nrm); }
 
 }  // extern "C"

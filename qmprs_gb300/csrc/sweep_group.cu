@@ -256,9 +256,10 @@ __device__ __forceinline__ void pass_flush(const float2 (&acc)[16], double2* red
 // hi = fp16(v s) and lo = fp16(v s - hi), both rounded to nearest (v s - hi
 // is exact in FP32); a product is lo_a hi_b + hi_a lo_b + hi_a hi_b.  With
 // 11-bit hi and lo the dropped lo_a lo_b and the rounding of lo leave a
-// relative error of about 3 * 2^-24 per product, as long as lo is a normal
-// FP16 number: the scale puts typical amplitudes near 16 and keeps every
-// |v s| <= 2^15 (below the FP16 maximum).  Fragments come straight from the
+// relative error of at most about 2^-21 per product (median about 2^-24),
+// the same as the 3xTF32 scheme, as long as lo is a normal FP16 number: the
+// scale puts typical amplitudes near 16 and keeps every |v s| <= 2^15
+// (below the FP16 maximum).  Fragments come straight from the
 // swizzled tile (no staging).
 __device__ __forceinline__ unsigned h2_bits(__half2 h) { return *reinterpret_cast<unsigned*>(&h); }
 
@@ -286,15 +287,6 @@ __device__ __forceinline__ void mma3(float (&c)[4], const unsigned (&ah)[4], con
   mma_f16(c, ah, bh[0], bh[1]);
 }
 
-// Scale of a state vector with 2^n amplitudes and norm `nrm`: 2^k with
-// 2^k nrm <= 2^min(n/2 + 4, 15), so |v s| <= 2^15 and typical amplitudes
-// (nrm 2^-n/2) land near 16.
-__device__ __forceinline__ float vec_scale(int n, double nrm) {
-  int e = 0;
-  frexp(nrm, &e);   // nrm < 2^e
-  const int top = n / 2 + 4 < 15 ? n / 2 + 4 : 15;
-  return ldexpf(1.f, top - e);
-}
 #define GATE_SCALE 256.f   // G entries (|g| <= 1) scaled into FP16's normal range
 
 // Cross matrix of one tile, accumulated into acc (scaled by sx sz).  A warp

@@ -86,3 +86,14 @@ QM_HD int apply_pos_offset(int p, int wmask, int rmask) {
   left &= ~p2;
   return ((p & 1) ? p0 : 0) | ((p & 2) ? p1 : 0) | ((p & 4) ? p2 : 0) | deposit32(p >> 3, left);
 }
+
+// Tensor-core scale of a state vector with 2^n amplitudes and norm `nrm`:
+// 2^k with 2^k nrm <= 2^min(n/2 + 4, 15), so every |v s| <= 2^15 (below
+// the FP16 maximum 65504) and typical amplitudes (nrm 2^-n/2) land near 16,
+// where the low half of the FP16 split is a normal number.
+QM_HD float vec_scale(int n, double nrm) {
+  int e = 0;
+  frexp(nrm, &e);   // nrm < 2^e
+  const int top = n / 2 + 4 < 15 ? n / 2 + 4 : 15;
+  return ldexpf(1.f, top - e);
+}

@@ -298,3 +298,18 @@ def test_gate_application_loads_and_stores_hit_distinct_banks(hc):
                 if consecutive:
                     assert _banks(addrs) == 16, (bin(wmask), e)
     assert worst >= 8
+
+
+def test_tensor_core_scale_keeps_fp16_in_range(hc):
+    """vec_scale: |v s| <= 2^15 for every amplitude of a vector of norm nrm
+    (|v| <= nrm), any size and norm, and the typical amplitude nrm 2^-n/2
+    lands in [2^2, 2^5] where it fits (n/2 + 4 <= 15)."""
+    hc.hc_vec_scale.restype = ctypes.c_float
+    hc.hc_vec_scale.argtypes = [ctypes.c_int, ctypes.c_double]
+    for n in range(2, 31):
+        for nrm in (1e-3, 0.37, 0.999999, 1.0, 1.000001, 3.0, 1e3):
+            s = hc.hc_vec_scale(n, nrm)
+            assert s > 0 and np.log2(s) == int(np.log2(s))   # a power of two
+            assert nrm * s <= 2.0 ** 15
+            if n // 2 + 4 <= 15:
+                assert 4.0 <= nrm * 2.0 ** (-n / 2) * s <= 32.0

@@ -52,9 +52,9 @@ UNIT = "states/s"
 # DRAM bytes (read + write) per algorithmic byte of a k_group_pass launch,
 # from an ncu capture of `python -m qmprs_gb300.profile_workload --states 32
 # --sweeps 1` (a group-1 launch: dram__bytes_read.sum + dram__bytes_write.sum
-# = 371.3 + 312.7 MB against 32 B x 23,195,648 amplitudes); a full-size
+# = 371.3 + 311.4 MB against 32 B x 23,195,648 amplitudes); a full-size
 # launch is scaled by its algorithmic bytes.
-PASS_DRAM_PER_ALG_BYTE = (371.317504e6 + 312.748544e6) / (32.0 * 23195648)
+PASS_DRAM_PER_ALG_BYTE = (371.333120e6 + 311.374848e6) / (32.0 * 23195648)
 
 
 def workload_spec(name: str, states: int, seed: int):

@@ -342,6 +342,32 @@ def iter_dioall(target: np.ndarray, n: int, num_layers: int, sweeps_per_layer: i
     return layers, fids
 
 
+def iter_dioi(target: np.ndarray, n: int, num_layers: int, sweeps_per_layer: int,
+              mode: str = "canonical") -> tuple[list[Layer], list[list[float]]]:
+    """Iter-DiOi schedule (arXiv:2209.00595; documented by the reference at
+    sequential.py:410-433 next to Iter-DiOall, not implemented there): k =
+    1..num_layers, disentangle one more layer from the residual r = C^H
+    |target>, sweep only that layer against r ``sweeps_per_layer`` times (the
+    older layers stay fixed; |<r|U|0>| is the whole circuit's fidelity), then
+    r <- U^H r.  Returns the layers (circuit order) and the per-step lists of
+    sweep fidelities."""
+    t = target / np.linalg.norm(target)
+    layers: list[Layer] = []            # circuit order
+    fids: list[list[float]] = []
+    residual = t.copy()
+    for _ in range(num_layers):
+        layer, _ = generate_layer(residual, n, mode)
+        newest = [layer]
+        step = []
+        for _ in range(sweeps_per_layer):
+            newest, f = sweep(residual, n, newest, mode)
+            step.append(f)
+        fids.append(step)
+        layers = newest + layers
+        residual = apply_inverse_layer(residual, n, newest[0])
+    return layers, fids
+
+
 @dataclass
 class EncodeResult:
     layers: list

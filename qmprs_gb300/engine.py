@@ -311,15 +311,22 @@ class Engine:
         return vec * torch.repeat_interleave(inv, counts)
 
     def encode_iterative(self, statevectors, bond_dimension: int, num_layers: int, sweeps_per_layer: int,
-                         nqubits=None) -> BatchResult:
-        """Iter-DiOall schedule (arXiv:2209.00595, documented by the
-        reference at qmprs/synthesis/mps_encoding/sequential.py:410-433):
-        for k = 1..num_layers, generate one analytic layer from the residual
-        C^H |target> of the current circuit (the newest layer is applied
-        first), then sweep all k layers `sweeps_per_layer` times.  Every state
-        gets all num_layers layers (no early exit).  ``sweep_fidelities``
-        holds the fidelity after every sweep, num_layers * sweeps_per_layer
-        columns."""
+                         nqubits=None, schedule: str = "iter_dioall") -> BatchResult:
+        """Iterative schedules (arXiv:2209.00595, documented by the reference
+        at qmprs/synthesis/mps_encoding/sequential.py:410-433): for k =
+        1..num_layers, generate one analytic layer from the residual
+        r = C^H |target> of the current circuit (the newest layer is applied
+        first), then sweep `sweeps_per_layer` times
+          "iter_dioall": all k layers against the target;
+          "iter_dioi":   the newest layer alone against r (the older layers
+                         stay fixed; its fidelity is the whole circuit's),
+                         then r <- U^H r.
+        Every state gets all num_layers layers (no early exit).
+        ``sweep_fidelities`` holds the fidelity after every sweep,
+        num_layers * sweeps_per_layer columns."""
+        if schedule not in ("iter_dioall", "iter_dioi"):
+            raise ValueError("schedule must be 'iter_dioall' or 'iter_dioi'.")
+        dioi = schedule == "iter_dioi"
         if nqubits is None:
             p, sv = self.upload(statevectors, num_layers, bond_dimension)
         else:
@@ -336,13 +343,21 @@ class Engine:
         g_rows = gates.view(-1, 32)
         fids = []
         residual = target.clone()
+        one = torch.ones(B, dtype=torch.int32, device="cuda")
         for k in range(L):
             g1, a1, _, _ = self.stage_layers(p, residual, 1, 1.0)
+            if dioi and S > 0:
+                # the newest layer alone, against the residual
+                sf, _ = self.stage_sweeps(p, residual, g1, a1, one, S, 0.0)
+                fids.append(sf[: B * S].view(B, S))
             src = torch.as_tensor(rows[0], device="cuda")
             dst = torch.as_tensor(rows[k], device="cuda")
             g_rows[dst] = g1.view(-1, 32)[src]
             arity[dst] = a1[src]
             nl.fill_(k + 1)
+            if dioi:
+                self.apply_layer(p, residual, gates, arity, k, True)   # r <- U_k^H r
+                continue
             if S > 0:
                 sf, _ = self.stage_sweeps(p, target, gates, arity, nl, S, 0.0)
                 fids.append(sf[: B * S].view(B, S))

@@ -164,12 +164,14 @@ class Sequential(MPSEncoder):
         starts the sweeps from the network's predicted layers; states that
         end below ``stop_fidelity`` fall back to the analytic layers.
         ``schedule`` (keyword only): ``"oall"`` (the reference's: all layers,
-        then ``num_sweeps`` sweeps) or ``"iter_dioall"`` (one layer at a time
+        then ``num_sweeps`` sweeps), ``"iter_dioall"`` (one layer at a time
         from the residual, each followed by ``num_sweeps`` sweeps of all
-        layers; arXiv:2209.00595, documented by the reference's sweep).
+        layers) or ``"iter_dioi"`` (one layer at a time, each followed by
+        ``num_sweeps`` sweeps of that layer alone against the residual);
+        arXiv:2209.00595, documented by the reference's sweep.
         """
-        if schedule not in ("oall", "iter_dioall"):
-            raise ValueError("schedule must be 'oall' or 'iter_dioall'.")
+        if schedule not in ("oall", "iter_dioall", "iter_dioi"):
+            raise ValueError("schedule must be 'oall', 'iter_dioall' or 'iter_dioi'.")
         if not isinstance(num_layers, int) or num_layers < 1:
             raise ValueError("The number of layers must be a positive integer.")
         if not isinstance(bond_dimension, int) or bond_dimension < 1:
@@ -179,8 +181,9 @@ class Sequential(MPSEncoder):
             ns = [int(n) for n in nqubits]
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
-            if schedule == "iter_dioall":
-                res = eng.encode_iterative(statevectors, bond_dimension, num_layers, num_sweeps, nqubits=ns)
+            if schedule != "oall":
+                res = eng.encode_iterative(statevectors, bond_dimension, num_layers, num_sweeps, nqubits=ns,
+                                           schedule=schedule)
             else:
                 res = eng.encode(statevectors, bond_dimension, num_layers, num_sweeps, self.fidelity_threshold,
                                  stop_fidelity, nqubits=ns, warm_start=warm_start)
@@ -189,8 +192,9 @@ class Sequential(MPSEncoder):
             ns = [k.num_qubits for k in kets]
             if any(n < 2 for n in ns):
                 raise ValueError("The statevector must have at least 2 qubits.")
-            if schedule == "iter_dioall":
-                res = eng.encode_iterative([k.data for k in kets], bond_dimension, num_layers, num_sweeps)
+            if schedule != "oall":
+                res = eng.encode_iterative([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
+                                           schedule=schedule)
             else:
                 res = eng.encode([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
                                  self.fidelity_threshold, stop_fidelity, warm_start=warm_start)

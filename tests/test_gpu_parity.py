@@ -146,6 +146,30 @@ def test_iter_dioall_matches_oracle(eng, ns, L, S_):
         assert abs(res.fidelity[b] - abs(np.vdot(psi, sv))) < FID_TOL
 
 
+@pytest.mark.parametrize("ns,L,S_", [([6, 7], 3, 2), ([9, 5], 2, 3)])
+def test_iter_dioi_matches_oracle(eng, ns, L, S_):
+    """Iter-DiOi schedule (the newest layer alone swept against the
+    residual): every sweep fidelity of every step, and the final overlap,
+    against the oracle's restatement; the API routes the schedule."""
+    svs = _svs(ns, 37)
+    res = eng.encode_iterative(svs, 64, L, S_, schedule="iter_dioi")
+    assert res.sweep_fidelities.shape == (len(ns), L * S_)
+    for b, sv in enumerate(svs):
+        n = ns[b]
+        t = _oracle_target(sv, 64)
+        layers, fids = D.iter_dioi(t, n, L, S_)
+        flat = [f for step in fids for f in step]
+        assert np.allclose(res.sweep_fidelities[b], flat, atol=FID_TOL), (res.sweep_fidelities[b], flat)
+        psi = D.circuit_state(layers, n)
+        assert abs(res.fidelity[b] - abs(np.vdot(psi, sv))) < FID_TOL
+    from qmprs_gb300.circuit import Circuit
+    from qmprs_gb300.synthesis.mps_encoding import Sequential
+    _, r2 = Sequential(Circuit).prepare_states(svs, 64, L, S_, emit=False, schedule="iter_dioi")
+    assert np.allclose(r2.sweep_fidelities, res.sweep_fidelities, atol=FID_TOL)
+    with pytest.raises(ValueError):
+        Sequential(Circuit).prepare_states(svs, 64, L, S_, emit=False, schedule="dioi")
+
+
 def test_sweeps_from_given_layers(eng):
     """_optimize_unitary_layers on oracle-made layers reproduces the oracle sweeps."""
     from qmprs_gb300.primitives import MPS

@@ -184,3 +184,28 @@ def test_iter_dioall_oracle_sweeps_never_lose_fidelity():
         assert all(b >= a - 1e-12 for a, b in zip(step, step[1:]))
     psi = D.circuit_state(layers, n)
     assert abs(abs(np.vdot(psi, t)) - fids[-1][-1]) < 1e-10
+
+
+def test_iter_dioi_oracle_sweeps_the_newest_layer_only():
+    """Iter-DiOi: within each step the sweeps of the newest layer do not
+    lower the fidelity, the last one is the whole circuit's overlap, the
+    older layers are left as they were, and without sweeps it builds the
+    same layers as Iter-DiOall."""
+    from oracle import states as S
+    n = 6
+    sv = S.random_mps(n, 4, 5)
+    t = sv / np.linalg.norm(sv)
+    layers, fids = D.iter_dioi(t, n, 3, 3)
+    for step in fids:
+        assert all(b >= a - 1e-12 for a, b in zip(step, step[1:]))
+    psi = D.circuit_state(layers, n)
+    assert abs(abs(np.vdot(psi, t)) - fids[-1][-1]) < 1e-10
+    two, _ = D.iter_dioi(t, n, 2, 3)
+    for a, b in zip(two, layers[1:]):   # the first two generated layers stay fixed
+        for (s1, e1, g1), (s2, e2, g2) in zip(a, b):
+            assert (s1, e1) == (s2, e2) and all(np.array_equal(x, y) for x, y in zip(g1, g2))
+    l0, _ = D.iter_dioi(t, n, 3, 0)
+    l1, _ = D.iter_dioall(t, n, 3, 0)
+    for a, b in zip(l0, l1):
+        for (s1, e1, g1), (s2, e2, g2) in zip(a, b):
+            assert (s1, e1) == (s2, e2) and all(np.allclose(x, y) for x, y in zip(g1, g2))

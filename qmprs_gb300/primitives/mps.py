@@ -49,6 +49,35 @@ class Tensor:
         return self.data.shape
 
 
+def _quimb_like(obj) -> bool:
+    """A quimb ``MatrixProductState``: site ``arrays`` and the index order
+    ``shape`` (a permutation of "lrp")."""
+    shape = getattr(obj, "shape", None)
+    return hasattr(obj, "arrays") and isinstance(shape, str) and sorted(shape) == ["l", "p", "r"]
+
+
+def _from_quimb(obj) -> "MatrixProductState":
+    """Site arrays of a quimb MPS in any index order, as (l, p, r) tensors.
+    The first site has no l index and the last no r index (quimb's open
+    boundary arrays)."""
+    arrays = [np.asarray(a) for a in obj.arrays]
+    n = len(arrays)
+    out = []
+    for i, a in enumerate(arrays):
+        letters = obj.shape
+        if n > 1 and i == 0:
+            letters = letters.replace("l", "")
+        if n > 1 and i == n - 1:
+            letters = letters.replace("r", "")
+        if n == 1:
+            letters = "p"
+        if a.ndim != len(letters):
+            raise ValueError(f"site {i}: array of rank {a.ndim} does not match the index order {obj.shape!r}")
+        want = "".join(c for c in "lpr" if c in letters)
+        out.append(np.transpose(a, [letters.index(c) for c in want]))
+    return MatrixProductState(out, layout="lpr")
+
+
 class MatrixProductState:
     """Site tensors of an open-boundary MPS with physical dimension 2.
 
@@ -148,6 +177,8 @@ class MPS:
             self._tensors, self._dense = self._from_statevector_dev(statevector, bond_dimension)
             self._form = "right"
         elif (mps is not None) and (statevector is None):
+            if not isinstance(mps, MatrixProductState) and _quimb_like(mps):
+                mps = _from_quimb(mps)
             if not isinstance(mps, MatrixProductState):
                 raise TypeError(
                     "`mps` must be a `MatrixProductState` instance. "

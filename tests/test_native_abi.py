@@ -39,3 +39,23 @@ def test_binding_covers_header():
 def test_version_call_needs_no_gpu():
     lib = _native.load()
     assert lib.qmprs_version() >= 100
+
+
+def _declared_arg_counts():
+    """Argument count of every declaration in the header."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for m in re.finditer(r"\b(qmprs_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_binding_argument_counts_match_header():
+    """The ctypes signature table passes exactly the arguments the header
+    declares for every entry point (a mismatch would shift pointers)."""
+    declared = _declared_arg_counts()
+    assert set(declared) == set(_native.SIGNATURES)
+    for name, (_, argtypes) in _native.SIGNATURES.items():
+        assert len(argtypes) == declared[name], (name, len(argtypes), declared[name])

@@ -95,6 +95,26 @@ int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, i
 int qmprs_plan_max_qubits(qmprs_plan_t p);
 
 /*
+ * Arithmetic of a plan's stages.  QMPRS_PRECISION_FAST (the default):
+ * complex64 statevector buffers, complex64 working states, split-FP16
+ * tensor-core products in the sweep.  QMPRS_PRECISION_EXACT: every
+ * statevector-sized caller buffer (the input of qmprs_mps_from_statevector
+ * and qmprs_plan_upload, the target, the circuit state, the inputs of
+ * qmprs_overlap and the vector of qmprs_apply_layer) is complex128, and the
+ * working states are double-float (about 2^-46 relative), so per-layer and
+ * per-sweep fidelities follow an FP64 run of the reference's algorithm to
+ * about 1e-9 even through deep layer stacks, whose bond-2 truncations
+ * amplify rounding by a few times per layer.  Set the precision before the
+ * first stage call; gates, tensors and fidelities keep their formats.
+ * Replaces: the complex128 numpy/quimb arithmetic of the reference
+ * (qmprs/primitives/mps.py, qmprs/synthesis/mps_encoding/sequential.py).
+ */
+#define QMPRS_PRECISION_FAST 0
+#define QMPRS_PRECISION_EXACT 1
+int qmprs_plan_set_precision(qmprs_plan_t p, int precision);
+int qmprs_plan_precision(qmprs_plan_t p);
+
+/*
  * Copy a packed complex64 statevector batch (`bytes` = vec_elems * 8, from
  * host memory, ideally pinned) into the plan's own device input buffer on
  * `stream` and return that buffer in *dev_out, ready for
@@ -126,7 +146,7 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv, int max_bond, dou
 /*
  * Dense statevector of an MPS held in the plan's tensor layout (site s of
  * state b at tensor_off[b] + s * 2 * chi_b^2, bonds as written by
- * qmprs_mps_from_statevector; every bond <= 64).
+ * qmprs_mps_from_statevector; every bond <= 1024).
  * Replaces: MPS.to_statevector (qmprs/primitives/mps.py:252-270), i.e.
  * quimb MatrixProductState.to_dense.
  */

@@ -61,3 +61,36 @@ def random_mps(n: int, bond: int, seed: int) -> np.ndarray:
         v = (v @ a.reshape(l, p * r)).reshape(-1, r)
     v = v.reshape(-1)
     return v / np.linalg.norm(v)
+
+
+def random_mps_batch(ns, bonds, seed: int, indices) -> list:
+    """Statevectors ``indices`` of the batch drawn by the product's batched
+    random-MPS generator (``qmprs_gb300.engine.Engine.random_mps_states``):
+    one generator seeded with ``seed`` draws every state's site tensors in
+    batch order (real then imaginary part per tensor), so the states are
+    replayed here in the same order, then left-canonicalised and contracted
+    in FP64 and normalised."""
+    rng = np.random.default_rng(seed)
+    want = set(int(i) for i in indices)
+    out = {}
+    for b, (n, bd) in enumerate(zip(ns, bonds)):
+        dims = [1] + [min(int(bd), 2 ** min(i, n - i)) for i in range(1, n)] + [1]
+        ts = []
+        for i in range(n):
+            shape = (dims[i], 2, dims[i + 1])
+            ts.append((rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2.0))
+        if b not in want:
+            continue
+        for i in range(n - 1):
+            l, p, r = ts[i].shape
+            q, rr = np.linalg.qr(ts[i].reshape(l * p, r))
+            ts[i] = q.reshape(l, p, q.shape[1])
+            nl, np_, nr = ts[i + 1].shape
+            ts[i + 1] = (rr @ ts[i + 1].reshape(nl, np_ * nr)).reshape(q.shape[1], np_, nr)
+        v = ts[0].reshape(2, -1)
+        for a in ts[1:]:
+            l, p, r = a.shape
+            v = (v @ a.reshape(l, p * r)).reshape(-1, r)
+        v = v.reshape(-1)
+        out[b] = v / np.linalg.norm(v)
+    return [out[int(i)] for i in indices]

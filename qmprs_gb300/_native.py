@@ -22,6 +22,10 @@ ERR_CUDA = 3
 ERR_NUMERIC = 4
 ERR_NONUNITARY = 5
 
+PRECISION_FAST = 0
+PRECISION_EXACT = 1
+PRECISIONS = {"fast": PRECISION_FAST, "exact": PRECISION_EXACT}
+
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_i64_p = ctypes.POINTER(ctypes.c_int64)
 _c_void_p = ctypes.c_void_p
@@ -41,6 +45,8 @@ SIGNATURES: dict[str, tuple] = {
     "qmprs_plan_destroy": (None, [_c_void_p]),
     "qmprs_plan_layout": (ctypes.c_int, [_c_void_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p, _c_i64_p]),
     "qmprs_plan_max_qubits": (ctypes.c_int, [_c_void_p]),
+    "qmprs_plan_set_precision": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
+    "qmprs_plan_precision": (ctypes.c_int, [_c_void_p]),
     "qmprs_plan_upload": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int64, _c_void_p, ctypes.POINTER(_c_void_p)]),
     "qmprs_mps_from_statevector": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int, ctypes.c_double, _c_void_p,
                                                   _c_void_p, _c_void_p, _c_void_p]),

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "exact.h"
 #include "internal.h"
 #include "qmprs_gb300.h"
 
@@ -63,6 +64,9 @@ struct qmprs_plan {
   double prof_ms[4] = {0, 0, 0, 0};
   double prof_bytes[4] = {0, 0, 0, 0};
   std::vector<int> gates_per_state;
+  // exact precision mode: double-float working states (allocated on first use)
+  int precision = QMPRS_PRECISION_FAST;
+  xc *X0 = nullptr, *X1 = nullptr, *X2 = nullptr, *XT = nullptr;
 };
 
 static std::atomic<long long> g_launches{0};
@@ -106,7 +110,7 @@ int check_kernel_errors(qmprs_plan* p, cudaStream_t s) {
     return set_err(p->h, QMPRS_ERR_NONUNITARY, "All the generated unitaries must be unitary.");
   if (flags & KERR_EIG_WIDTH)
     return set_err(p->h, QMPRS_ERR_UNSUPPORTED,
-                   "a bond of the MPS exceeds the supported width (bond > 64)");
+                   "a bond of the MPS exceeds the supported width (bond > 1024)");
   if (flags & KERR_NONFINITE) return set_err(p->h, QMPRS_ERR_NUMERIC, "non-finite environment in a sweep");
   if (flags & KERR_BAD_GATE)
     return set_err(p->h, QMPRS_ERR_INVALID, "a gate slot has an invalid arity or position (gates skipped)");
@@ -209,6 +213,246 @@ void launch_wide_contract(qmprs_plan* p, int step, const double2* tensors, const
   }
 }
 
+// ---- exact precision mode: orchestration ---------------------------------------------
+//
+// The same stages as the fast mode, on double-float working states (exact.cu).
+// Caller-facing statevector buffers are complex128.  Stage (a) runs state by
+// state with the bonds read on the host after every cut; the layer stage and
+// the sweeps batch all states in every launch like the fast mode, with one
+// gate per launch.
+
+namespace {
+
+int ensure_tt_scratch(qmprs_plan* p) {
+  if (p->tt_partials) return QMPRS_OK;
+  const int64_t WW = (int64_t)p->tt_w * p->tt_w;
+  CK(dalloc(&p->tt_partials, (int64_t)p->B * TT_SPLIT * WW));
+  CK(dalloc(&p->gram, (int64_t)p->B * WW));
+  CK(dalloc(&p->vsel2, (int64_t)p->B * WW));
+  CK(dalloc(&p->vwork, (int64_t)p->B * WW));
+  if (p->tt_b > TT_MAXB) {
+    CK(cudaMalloc(reinterpret_cast<void**>(&p->d_wj_rot), wj_rot_bytes(p->tt_w)));
+    CK(dalloc(&p->d_wj_count, 1));
+    CK(dalloc(&p->d_wj_trace, 1));
+    CK(dalloc(&p->d_wj_perm, p->tt_w));
+    CK(dalloc(&p->d_wj_lam, p->tt_w));
+  }
+  return QMPRS_OK;
+}
+
+int ensure_exact(qmprs_plan* p) {
+  if (p->X0) return QMPRS_OK;
+  CK(dalloc(&p->X0, p->vec_total));
+  CK(dalloc(&p->X1, p->vec_total));
+  CK(dalloc(&p->X2, p->vec_total));
+  CK(dalloc(&p->XT, p->vec_total));
+  return QMPRS_OK;
+}
+
+int read_ints(qmprs_plan* p, const int* dev, std::vector<int>& host, cudaStream_t s) {
+  CK(cudaMemcpyAsync(host.data(), dev, sizeof(int) * host.size(), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return QMPRS_OK;
+}
+
+// Dense statevector of the MPS in `tensors` (bonds hb on the host), left to
+// right in double-float: X_1 = A_0, X_{c+1} = X_c A_c, into `out`.  With
+// `start` (stage (a)), state b starts instead from X_c = f_b Y_c at
+// c = start[b], where Y_c = M_c V_c is the projected remainder saved in
+// `saved` and f_b (device, `scale`) the norm factor of site 0: when no cut
+// left of c truncates, every kept space there holds the remainder's whole
+// row space, so A_0 ... A_{c-1} contract to exactly that, and the
+// rank-deficient left cuts (2^c rows, more columns) add no rounding of
+// their eigenvectors to the target.
+void x_contract(qmprs_plan* p, const double2* tensors, const std::vector<int>& hb, xc* out, cudaStream_t s,
+                const std::vector<int>* start = nullptr, const xc* saved = nullptr, const double* scale = nullptr) {
+  const int stride = p->max_n + 1;
+  for (int b = 0; b < p->B; ++b) {
+    const int n = p->n[b];
+    const int* bb = hb.data() + (size_t)b * stride;
+    bool ok = true;
+    for (int c = 0; c <= n; ++c) ok = ok && bb[c] >= 1 && bb[c] <= p->tt_b;
+    if (!ok) continue;
+    const int ce = chi_eff_host(p->max_bond, n);
+    const double2* t0 = tensors + p->tensor_off[b];
+    xc* cur = p->X0 + p->vec_off[b];
+    xc* nxt = p->X1 + p->vec_off[b];
+    int c_first = 1;
+    if (start && (*start)[b] >= 1) {
+      c_first = (*start)[b];
+      launch_x_scale_flat(saved + p->vec_off[b], cur, ipow2(c_first) * bb[c_first], scale + b, s);
+    } else {
+      launch_x_from_d_flat(t0, cur, 2 * (int64_t)bb[1], s);
+    }
+    for (int c = c_first; c <= n - 1; ++c) {
+      const int rc = bb[c], rn = bb[c + 1];
+      const double2* a = t0 + (int64_t)c * 2 * ce * ce;
+      xc* o = c == n - 1 ? out + p->vec_off[b] : nxt;
+      launch_x_gemm(cur, rc, a, 2 * rn, o, 2 * rn, ipow2(c), 2 * rn, rc, s);
+      std::swap(cur, nxt);
+    }
+  }
+}
+
+int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, double cutoff, double2* tensors,
+                               int* bonds, double2* target, cudaStream_t s) {
+  int rc = ensure_tt_scratch(p);
+  if (rc == QMPRS_OK) rc = ensure_exact(p);
+  if (rc != QMPRS_OK) return rc;
+  const int64_t WW = (int64_t)p->tt_w * p->tt_w;
+  const int stride = p->max_n + 1;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  CK(cudaMemcpyAsync(bonds, p->d_bond_init, sizeof(int) * (size_t)p->B * stride, cudaMemcpyDeviceToDevice, s));
+  launch_x_from_d(p->bd, sv, p->X0, s);
+  launch_x_dot(p->bd, p->X0, p->X0, p->partials, p->sq, s);
+  std::vector<double2> sq(p->B);
+  CK(cudaMemcpyAsync(sq.data(), p->sq, sizeof(double2) * p->B, cudaMemcpyDeviceToHost, s));
+  std::vector<int> hb((size_t)p->B * stride), start(p->B, -1);
+  xc* buf[2] = {p->X1, p->X2};
+  for (int j = 0; j + 2 <= p->max_n; ++j) {
+    if ((rc = read_ints(p, bonds, hb, s)) != QMPRS_OK) return rc;
+    const xc* src = j == 0 ? p->X0 : buf[(j - 1) & 1];
+    bool wide = false;
+    for (int b = 0; b < p->B; ++b) {
+      const int c = p->n[b] - 1 - j;
+      if (c < 1) continue;
+      const int r = hb[(size_t)b * stride + c + 1];
+      if (r < 1 || r > p->tt_b) continue;
+      launch_x_gram(src + p->vec_off[b], ipow2(c), 2 * r, p->tt_partials + (int64_t)b * TT_SPLIT * WW, WW,
+                    p->gram + (int64_t)b * WW, s);
+      wide = wide || 2 * r > TT_MAXW;
+    }
+    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond, s);
+    if (wide) {
+      for (int b = 0; b < p->B; ++b) {
+        const int c = p->n[b] - 1 - j;
+        if (c < 1) continue;
+        const int r = hb[(size_t)b * stride + c + 1];
+        if (r < 1 || r > p->tt_b || 2 * r <= TT_MAXW) continue;
+        const int e = tt_wide_eig(p->bd, b, c, 2 * r, p->gram, p->vwork, p->d_wj_rot, p->d_wj_count, p->d_wj_trace,
+                                  p->d_wj_perm, p->d_wj_lam, bonds, p->vsel2, tensors, p->max_bond, max_bond, cutoff,
+                                  s);
+        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) device-wide Jacobi");
+      }
+    }
+    if ((rc = read_ints(p, bonds, hb, s)) != QMPRS_OK) return rc;
+    for (int b = 0; b < p->B; ++b) {
+      const int c = p->n[b] - 1 - j;
+      if (c < 1) continue;
+      const int r = hb[(size_t)b * stride + c + 1], keep = hb[(size_t)b * stride + c];
+      if (r < 1 || keep < 1 || r > p->tt_b || keep > p->tt_b) continue;
+      launch_x_gemm(src + p->vec_off[b], 2 * r, p->vsel2 + (int64_t)b * WW, p->tt_b, buf[j & 1] + p->vec_off[b],
+                    keep, ipow2(c), keep, 2 * r, s);
+      // the last cut (so far, right to left) that truncates, or the first
+      // cut: the target's contraction starts from its projected remainder
+      if (c == p->n[b] - 1 || keep < std::min<int64_t>(ipow2(c), 2 * r)) {
+        CK(cudaMemcpyAsync(p->XT + p->vec_off[b], buf[j & 1] + p->vec_off[b], sizeof(xc) * ipow2(c) * keep,
+                           cudaMemcpyDeviceToDevice, s));
+        start[b] = c;
+      }
+    }
+  }
+  for (int b = 0; b < p->B; ++b) {
+    const int r1 = hb[(size_t)b * stride + 1];
+    if (r1 < 1 || r1 > p->tt_b) continue;
+    launch_x_site0(buf[(p->n[b] - 2) & 1] + p->vec_off[b], r1, sq[b].x, tensors + p->tensor_off[b], p->nuc + b, s);
+  }
+  x_contract(p, tensors, hb, p->XT, s, &start, p->XT, p->nuc);
+  launch_x_to_d(p->bd, p->XT, target, s);
+  return check_kernel_errors(p, s);
+}
+
+int exact_unitary_layers(qmprs_plan* p, const double2* target, int num_layers, double fidelity_threshold,
+                         double2* gates, signed char* ar, int* layers_out, double2* layer_fid, cudaStream_t s) {
+  int rc = ensure_exact(p);
+  if (rc != QMPRS_OK) return rc;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(layers_out, 0, sizeof(int) * p->B, s));
+  CK(cudaMemsetAsync(layer_fid, 0, sizeof(double2) * (size_t)p->B * num_layers, s));
+  launch_fill_int(p->active, p->B, 1, s);
+  xc* work = p->X0;
+  launch_x_from_d(p->bd, target, work, s);
+  launch_x_normalize(p->bd, work, work, p->partials, p->sq, s);
+  xc* buf[2] = {p->X1, p->X2};
+  const double atol = 1.0 - fidelity_threshold;
+  const int64_t nb = (int64_t)p->B * (p->max_n + 1);
+  for (int l = 0; l < num_layers; ++l) {
+    CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
+    for (int j = 0; j + 2 <= p->max_n; ++j) {
+      const xc* src = j == 0 ? work : buf[(j - 1) & 1];
+      launch_x_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->active, s);
+      launch_layer_eig(p->bd, j, p->partials, p->vsel, p->bonds, p->site_t, p->active, s);
+      launch_x_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s);
+    }
+    launch_x_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s);
+    for (int st = 0; st < p->max_n; ++st) {
+      GateSel sel{SEL_INVERSE, st, l, 1, gates, ar, nullptr, p->active};
+      launch_x_apply_gate(p->bd, work, sel, s);
+    }
+    launch_x_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
+    launch_count_active(p->B, p->active, p->num_active, s);
+    int na = 0;
+    CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (na == 0) break;
+  }
+  return check_kernel_errors(p, s);
+}
+
+int exact_optimize_layers(qmprs_plan* p, const double2* target, double2* gates, const signed char* ar,
+                          const int* num_layers, int num_sweeps, double stop_fidelity, double* sweep_fid,
+                          int* sweeps_done, cudaStream_t s) {
+  int rc = ensure_exact(p);
+  if (rc != QMPRS_OK) return rc;
+  int max_gates = 0;
+  if ((rc = read_max_gates(p, num_layers, s, &max_gates)) != QMPRS_OK) return rc;
+  launch_fill_int(p->active, p->B, 1, s);
+  launch_x_from_d(p->bd, target, p->XT, s);
+  launch_x_dot(p->bd, p->XT, p->XT, p->partials, p->tnorm, s);
+  xc* psi = p->X0;
+  xc* t = p->X1;
+  for (int sw = 0; sw < num_sweeps; ++sw) {
+    launch_x_zero(p->bd, psi, p->active, s);
+    for (int j = 0; j < max_gates; ++j) {
+      GateSel sel{SEL_REBUILD, j, 0, 0, gates, ar, num_layers, p->active};
+      launch_x_apply_gate(p->bd, psi, sel, s);
+    }
+    launch_x_copy(p->bd, p->XT, t, p->active, s);
+    for (int j = 0; j < max_gates; ++j) {
+      launch_x_sweep_step(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
+      GateSel sel{SEL_SWEEP, j, 0, 1, gates, ar, num_layers, p->active};
+      launch_x_apply_gate(p->bd, t, sel, s);
+    }
+    CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));
+    launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active, stop_fidelity,
+                        p->num_active, s);
+    if (stop_fidelity > 0.0) {
+      int na = 0;
+      CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (na == 0) break;
+    }
+  }
+  return check_kernel_errors(p, s);
+}
+
+int exact_circuit_state(qmprs_plan* p, const double2* gates, const signed char* ar, const int* num_layers,
+                        double2* out, cudaStream_t s) {
+  int rc = ensure_exact(p);
+  if (rc != QMPRS_OK) return rc;
+  int max_gates = 0;
+  if ((rc = read_max_gates(p, num_layers, s, &max_gates)) != QMPRS_OK) return rc;
+  launch_x_zero(p->bd, p->X0, nullptr, s);
+  for (int j = 0; j < max_gates; ++j) {
+    GateSel sel{SEL_REBUILD, j, 0, 0, gates, ar, num_layers, nullptr};
+    launch_x_apply_gate(p->bd, p->X0, sel, s);
+  }
+  launch_x_to_d(p->bd, p->X0, out, s);
+  return check_kernel_errors(p, s);
+}
+
+}  // namespace
+
 extern "C" {
 
 int qmprs_version(void) { return 100; }
@@ -261,7 +505,7 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
                   p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials,
                   p->d_rgrp,   p->d_nrgroups,   p->d_wj_rot,  p->d_wj_count,  p->d_wj_perm,
-                  p->d_wj_trace, p->d_wj_lam, p->d_input};
+                  p->d_wj_trace, p->d_wj_lam, p->d_input, p->X0, p->X1, p->X2, p->XT};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -447,12 +691,23 @@ int qmprs_plan_layout(qmprs_plan_t p, int64_t* vec_elems, int64_t* gate_elems, i
 
 int qmprs_plan_max_qubits(qmprs_plan_t p) { return p ? p->max_n : -1; }
 
+int qmprs_plan_set_precision(qmprs_plan_t p, int precision) {
+  if (!p) return QMPRS_ERR_INVALID;
+  if (precision != QMPRS_PRECISION_FAST && precision != QMPRS_PRECISION_EXACT)
+    return set_err(p->h, QMPRS_ERR_INVALID, "precision must be QMPRS_PRECISION_FAST or QMPRS_PRECISION_EXACT");
+  p->precision = precision;
+  return QMPRS_OK;
+}
+
+int qmprs_plan_precision(qmprs_plan_t p) { return p ? p->precision : -1; }
+
 int qmprs_plan_upload(qmprs_plan_t p, const void* host, int64_t bytes, void* stream, void** dev_out) {
   if (!p || !host || !dev_out) return QMPRS_ERR_INVALID;
   *dev_out = nullptr;
-  if (bytes != p->vec_total * (int64_t)sizeof(float2))
+  const int64_t elem = p->precision == QMPRS_PRECISION_EXACT ? (int64_t)sizeof(double2) : (int64_t)sizeof(float2);
+  if (bytes != p->vec_total * elem)
     return set_err(p->h, QMPRS_ERR_INVALID, "packed statevector buffer does not match the qubit counts");
-  if (!p->d_input) CK(cudaMalloc(&p->d_input, (size_t)bytes));
+  if (!p->d_input) CK(cudaMalloc(&p->d_input, (size_t)p->vec_total * sizeof(double2)));
   // Pinned, device-mapped host memory is read by a copy kernel (k_upload);
   // anything else goes through the copy engine.
   cudaPointerAttributes at{};
@@ -480,20 +735,13 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
     if (chi_eff_host(max_bond, p->n[b]) > TT_WIDE_MAXB)
       return set_err(p->h, QMPRS_ERR_UNSUPPORTED,
                      "statevector -> MPS supports bond dimensions up to 1024 (min(bond_dimension, 2^(n/2)) > 1024)");
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    return exact_mps_from_statevector(p, (const double2*)sv_, max_bond, cutoff, tensors, bonds, (double2*)target_, s);
   const int64_t WW = (int64_t)p->tt_w * p->tt_w;
   const bool wide = p->tt_b > TT_MAXB;
-  if (!p->tt_partials) {
-    CK(dalloc(&p->tt_partials, (int64_t)p->B * TT_SPLIT * WW));
-    CK(dalloc(&p->gram, (int64_t)p->B * WW));
-    CK(dalloc(&p->vsel2, (int64_t)p->B * WW));
-    CK(dalloc(&p->vwork, (int64_t)p->B * WW));
-    if (wide) {
-      CK(cudaMalloc(reinterpret_cast<void**>(&p->d_wj_rot), wj_rot_bytes(p->tt_w)));
-      CK(dalloc(&p->d_wj_count, 1));
-      CK(dalloc(&p->d_wj_trace, 1));
-      CK(dalloc(&p->d_wj_perm, p->tt_w));
-      CK(dalloc(&p->d_wj_lam, p->tt_w));
-    }
+  {
+    const int rc = ensure_tt_scratch(p);
+    if (rc != QMPRS_OK) return rc;
   }
   CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
   const int64_t nb = (int64_t)p->B * (p->max_n + 1);
@@ -562,6 +810,22 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
 int qmprs_mps_to_statevector(qmprs_plan_t p, const void* tensors, const int* bonds, void* out, void* stream) {
   if (!p || !tensors || !bonds || !out) return QMPRS_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  if (p->precision == QMPRS_PRECISION_EXACT) {
+    int rc = ensure_exact(p);
+    if (rc != QMPRS_OK) return rc;
+    std::vector<int> hbx((size_t)p->B * (p->max_n + 1));
+    if ((rc = read_ints(p, bonds, hbx, s)) != QMPRS_OK) return rc;
+    for (int b = 0; b < p->B; ++b)
+      for (int c = 0; c <= p->n[b]; ++c) {
+        const int r = hbx[(size_t)b * (p->max_n + 1) + c];
+        if (r < 1 || r > chi_eff_host(p->max_bond, p->n[b]) || (c > 0 && c < p->n[b] && r > (1 << std::min(c, p->n[b] - c))))
+          return set_err(p->h, QMPRS_ERR_INVALID, "a bond of the MPS is out of range for the plan");
+      }
+    x_contract(p, (const double2*)tensors, hbx, p->XT, s);
+    launch_x_to_d(p->bd, p->XT, (double2*)out, s);
+    return check_kernel_errors(p, s);
+  }
   float2* buf[2] = {p->S0, p->S1};
   const bool wide = p->tt_b > TT_MAXB;
   std::vector<int> hb(wide ? (size_t)p->B * (p->max_n + 1) : 0);
@@ -574,8 +838,7 @@ int qmprs_mps_to_statevector(qmprs_plan_t p, const void* tensors, const int* bon
     launch_mps_contract(p->bd, j, (const double2*)tensors, bonds, p->max_bond, src, buf[j & 1], (float2*)out, s);
     if (wide) launch_wide_contract(p, j, (const double2*)tensors, hb, src, buf[j & 1], (float2*)out, s);
   }
-  CK(cudaGetLastError());
-  return QMPRS_OK;
+  return check_kernel_errors(p, s);
 }
 
 int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, double fidelity_threshold,
@@ -586,6 +849,9 @@ int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, do
   if (!(fidelity_threshold >= 0.0 && fidelity_threshold <= 1.0))
     return set_err(p->h, QMPRS_ERR_INVALID, "The fidelity threshold must be a float between 0 and 1.");
   cudaStream_t s = (cudaStream_t)stream;
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    return exact_unitary_layers(p, (const double2*)target_, num_layers, fidelity_threshold, (double2*)gates_,
+                                (signed char*)arity, layers_out, (double2*)layer_fid_, s);
   const float2* target = (const float2*)target_;
   double2* gates = (double2*)gates_;
   signed char* ar = (signed char*)arity;
@@ -637,6 +903,9 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   CK(cudaMemsetAsync(sweeps_done, 0, sizeof(int) * p->B, s));
   if (num_sweeps == 0) return QMPRS_OK;
   CK(cudaMemsetAsync(sweep_fid, 0, sizeof(double) * (size_t)p->B * num_sweeps, s));
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    return exact_optimize_layers(p, (const double2*)target_, (double2*)gates_, (const signed char*)arity, num_layers,
+                                 num_sweeps, stop_fidelity, sweep_fid, sweeps_done, s);
   int max_gates = 0;
   int rc = read_max_gates(p, num_layers, s, &max_gates);
   if (rc != QMPRS_OK) return rc;
@@ -713,6 +982,8 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
   if (!p || !gates || !arity || !num_layers || !out) return QMPRS_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    return exact_circuit_state(p, (const double2*)gates, (const signed char*)arity, num_layers, (double2*)out, s);
   int max_gates = 0;
   int rc = read_max_gates(p, num_layers, s, &max_gates);
   if (rc != QMPRS_OK) return rc;
@@ -737,7 +1008,10 @@ int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, 
 int qmprs_overlap(qmprs_plan_t p, const void* a, const void* b, void* out, void* stream) {
   if (!p || !a || !b || !out) return QMPRS_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  launch_overlap(p->bd, (const float2*)a, (const float2*)b, p->partials, (double2*)out, s);
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    launch_d_dot(p->bd, (const double2*)a, (const double2*)b, p->partials, (double2*)out, s);
+  else
+    launch_overlap(p->bd, (const float2*)a, (const float2*)b, p->partials, (double2*)out, s);
   CK(cudaGetLastError());
   return QMPRS_OK;
 }
@@ -747,8 +1021,21 @@ int qmprs_apply_layer(qmprs_plan_t p, void* vec, const void* gates, const int8_t
   if (!p || !vec || !gates || !arity) return QMPRS_ERR_INVALID;
   if (layer < 0 || layer >= p->max_layers) return set_err(p->h, QMPRS_ERR_INVALID, "layer index out of range");
   cudaStream_t s = (cudaStream_t)stream;
-  const int mode = inverse ? ORDER_LAYER_INV : ORDER_LAYER_FWD;
   const signed char* ar = (const signed char*)arity;
+  if (p->precision == QMPRS_PRECISION_EXACT) {
+    const int rc = ensure_exact(p);
+    if (rc != QMPRS_OK) return rc;
+    CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+    launch_x_from_d(p->bd, (const double2*)vec, p->X0, s);
+    for (int st = 0; st < p->max_n; ++st) {
+      GateSel sel{inverse ? SEL_INVERSE : SEL_LAYER_FWD, st, layer, inverse ? 1 : 0, (const double2*)gates, ar, nullptr,
+                  nullptr};
+      launch_x_apply_gate(p->bd, p->X0, sel, s);
+    }
+    launch_x_to_d(p->bd, p->X0, (double2*)vec, s);
+    return check_kernel_errors(p, s);
+  }
+  const int mode = inverse ? ORDER_LAYER_INV : ORDER_LAYER_FWD;
   launch_layer_plan(p->bd, p->gd, ar, mode, layer, nullptr, s);
   for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
     launch_rebuild_pass(p->bd, p->gd, r, (float2*)vec, (const double2*)gates, ar, nullptr, nullptr, s, mode, layer,

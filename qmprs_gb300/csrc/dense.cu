@@ -148,12 +148,16 @@ void launch_apply_gate(const BatchDev& bd, float2* vec, const GateSel& sel, cuda
   k_apply_gate<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, vec, sel);
 }
 
+void launch_reduce_tiles(const BatchDev& bd, const double2* partials, double2* out, cudaStream_t s) {
+  qm_note_launch();
+  k_reduce_tiles<<<(bd.B + 7) / 8, 256, 0, s>>>(bd, partials, out);
+}
+
 void launch_overlap(const BatchDev& bd, const float2* a, const float2* b, double2* partials,
                     double2* out, cudaStream_t s) {
   qm_note_launch();
   k_overlap<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, a, b, partials, out);
-  qm_note_launch();
-  k_reduce_tiles<<<(bd.B + 7) / 8, 256, 0, s>>>(bd, partials, out);
+  launch_reduce_tiles(bd, partials, out, s);
 }
 
 // dst = src / ||src||; sq[b].x receives ||src||^2

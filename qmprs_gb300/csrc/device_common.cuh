@@ -100,6 +100,15 @@ __device__ __forceinline__ bool last_tile_ticket(int* ticket, int b, int nt) {
 
 __device__ __forceinline__ double2 ld_cg(const double2* p) { return __ldcg(p); }
 
+// Tiles of a state that take part in the layer stage's Gram of a 2^c-row
+// remainder: at least 4096 rows (16 per thread) each, so a short remainder
+// is not spread over every tile of the state, each paying a full fp64 warp
+// reduction.  The eigen kernel sums the partials of exactly these tiles.
+__device__ __forceinline__ int layer_gram_tiles(int c, int nt) {
+  const int64_t want = ((((int64_t)1) << c) + 4095) >> 12;
+  return want < nt ? (int)want : nt;
+}
+
 // Index of amplitude for quad r on bits (hi, lo = hi - 1), with values (bh, bl).
 __device__ __forceinline__ int64_t quad_base(int64_t r, int lo) {
   return ((r >> lo) << (lo + 2)) | (r & ((((int64_t)1) << lo) - 1));

@@ -133,6 +133,8 @@ void launch_apply_gate(const BatchDev& bd, float2* vec, const GateSel& sel, cuda
 void launch_upload(void* dst, const void* src_dev, int64_t bytes, cudaStream_t s);
 void launch_overlap(const BatchDev& bd, const float2* a, const float2* b, double2* partials,
                     double2* out, cudaStream_t s);
+// out[b] = sum of one partial per tile of state b (fixed order)
+void launch_reduce_tiles(const BatchDev& bd, const double2* partials, double2* out, cudaStream_t s);
 void launch_copy_normalize(const BatchDev& bd, const float2* src, float2* dst, double2* partials,
                            double2* sq_norms, cudaStream_t s);
 
@@ -140,6 +142,8 @@ void launch_copy_normalize(const BatchDev& bd, const float2* src, float2* dst, d
 void launch_layer_gram(const BatchDev& bd, int step, const float2* work, const float2* src,
                        const int* bonds, double2* partials, double2* vsel, int* bonds_out,
                        double2* site_t, const int* active, cudaStream_t s);
+void launch_layer_eig(const BatchDev& bd, int step, const double2* partials, double2* vsel, int* bonds,
+                      double2* site_t, const int* active, cudaStream_t s);
 void launch_layer_project(const BatchDev& bd, int step, const float2* work, const float2* src,
                           float2* dst, const int* bonds, const double2* vsel, const int* active,
                           cudaStream_t s);

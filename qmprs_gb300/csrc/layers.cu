@@ -55,14 +55,6 @@ __device__ __forceinline__ void gram_rows(const float2* m, int64_t lo, int64_t h
   }
 }
 
-// Tiles of a state that take part in the Gram of a 2^c-row remainder: at
-// least 4096 rows (16 per thread) each, so a short remainder is not spread
-// over every tile of the state, each paying a full fp64 warp reduction.
-__device__ __forceinline__ int layer_gram_tiles(int c, int nt) {
-  const int64_t want = ((((int64_t)1) << c) + 4095) >> 12;
-  return want < nt ? (int)want : nt;
-}
-
 __global__ void __launch_bounds__(BLOCK_THREADS) k_layer_gram(BatchDev bd, int step, const float2* work,
                                                               const float2* src, const int* bonds,
                                                               double2* partials, const int* active) {
@@ -256,9 +248,14 @@ void launch_layer_gram(const BatchDev& bd, int step, const float2* work, const f
   (void)bonds;
   qm_note_launch();
   k_layer_gram<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, step, work, src, bonds_out, partials, active);
+  launch_layer_eig(bd, step, partials, vsel, bonds_out, site_t, active, s);
+}
+
+void launch_layer_eig(const BatchDev& bd, int step, const double2* partials, double2* vsel, int* bonds,
+                      double2* site_t, const int* active, cudaStream_t s) {
   qm_note_launch();
   const int blocks = bd.B < 152 * 8 ? bd.B : 152 * 8;
-  k_layer_eig<<<blocks, BLOCK_THREADS, 0, s>>>(bd, step, partials, vsel, bonds_out, site_t, active);
+  k_layer_eig<<<blocks, BLOCK_THREADS, 0, s>>>(bd, step, partials, vsel, bonds, site_t, active);
 }
 
 void launch_layer_project(const BatchDev& bd, int step, const float2* work, const float2* src,

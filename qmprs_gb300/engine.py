@@ -65,25 +65,33 @@ class _DeviceBuffer:
     """A float32 device array owned by the library (a plan buffer), exposed
     to torch through the CUDA array interface without a copy."""
 
-    def __init__(self, ptr: int, numel: int):
-        self.__cuda_array_interface__ = {"shape": (int(numel),), "typestr": "<f4", "data": (int(ptr), False),
+    def __init__(self, ptr: int, numel: int, typestr: str = "<f4"):
+        self.__cuda_array_interface__ = {"shape": (int(numel),), "typestr": typestr, "data": (int(ptr), False),
                                          "version": 3, "strides": None}
 
 
 class Plan:
-    """A batch layout: offsets of every state in the caller buffers."""
+    """A batch layout: offsets of every state in the caller buffers.
 
-    def __init__(self, hd: Handle, nqubits: list[int], max_layers: int, max_bond: int):
+    ``precision`` "fast": complex64 statevector buffers (float32 pairs);
+    "exact": complex128 buffers (float64 pairs) and double-float working
+    states (``QMPRS_PRECISION_EXACT``)."""
+
+    def __init__(self, hd: Handle, nqubits: list[int], max_layers: int, max_bond: int, precision: str = "fast"):
         self.hd = hd
         self.lib = hd.lib
         self.nqubits = [int(n) for n in nqubits]
         self.B = len(self.nqubits)
         self.max_layers = int(max_layers)
         self.max_bond = int(max_bond)
+        if precision not in _native.PRECISIONS:
+            raise ValueError("precision must be 'fast' or 'exact'.")
+        self.precision = precision
         arr = (ctypes.c_int * self.B)(*self.nqubits)
         p = ctypes.c_void_p()
         hd.check(self.lib.qmprs_plan_create(hd.h, self.B, arr, self.max_layers, self.max_bond, ctypes.byref(p)))
         self.p = p
+        hd.check(self.lib.qmprs_plan_set_precision(p, _native.PRECISIONS[precision]))
         ve, ge, te = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         vo = (ctypes.c_int64 * self.B)()
         go = (ctypes.c_int64 * self.B)()
@@ -94,6 +102,19 @@ class Plan:
         self.gate_off = np.array(go[:], dtype=np.int64)
         self.tensor_off = np.array(to[:], dtype=np.int64)
         self.max_n = self.lib.qmprs_plan_max_qubits(p)
+
+    @property
+    def vdtype(self):
+        """Real dtype of the statevector-sized buffers (two entries per amplitude)."""
+        return torch.float64 if self.precision == "exact" else torch.float32
+
+    @property
+    def npdtype(self):
+        return np.complex128 if self.precision == "exact" else np.complex64
+
+    def vec(self) -> torch.Tensor:
+        """An uninitialised statevector-sized device buffer of this plan."""
+        return torch.empty(self.vec_elems * 2, dtype=self.vdtype, device="cuda")
 
     def chi_eff(self, b: int) -> int:
         return min(self.max_bond, 2 ** (self.nqubits[b] // 2))
@@ -173,17 +194,17 @@ class Engine:
         self.lib = self.hd.lib
         self._plans: dict = {}
 
-    def plan(self, nqubits, max_layers: int, max_bond: int) -> Plan:
-        key = (tuple(int(n) for n in nqubits), int(max_layers), int(max_bond))
+    def plan(self, nqubits, max_layers: int, max_bond: int, precision: str = "fast") -> Plan:
+        key = (tuple(int(n) for n in nqubits), int(max_layers), int(max_bond), precision)
         p = self._plans.get(key)
         if p is None:
-            p = Plan(self.hd, list(key[0]), key[1], key[2])
+            p = Plan(self.hd, list(key[0]), key[1], key[2], precision)
             self._plans[key] = p
         return p
 
     @staticmethod
-    def pack(statevectors) -> tuple[list[int], np.ndarray]:
-        """Concatenate complex statevectors (already Ket-normalised) as complex64."""
+    def pack(statevectors, dtype=np.complex64) -> tuple[list[int], np.ndarray]:
+        """Concatenate complex statevectors (already Ket-normalised) as ``dtype``."""
         ns, parts = [], []
         for v in statevectors:
             v = np.asarray(v).reshape(-1)
@@ -191,16 +212,16 @@ class Engine:
             if 2 ** n != v.size:
                 raise ValueError("statevector length must be a power of two")
             ns.append(n)
-            parts.append(v.astype(np.complex64))
+            parts.append(v.astype(dtype))
         return ns, np.concatenate(parts)
 
     # ---- stages --------------------------------------------------------------
-    def upload(self, statevectors, max_layers: int, max_bond: int):
+    def upload(self, statevectors, max_layers: int, max_bond: int, precision: str = "fast"):
         """Plan the batch and copy the (Ket-normalised) statevectors to the device."""
-        ns, host = self.pack(statevectors)
-        p = self.plan(ns, max_layers, max_bond)
-        pinned = torch.from_numpy(host.view(np.float32)).pin_memory()
-        sv = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        ns, host = self.pack(statevectors, np.complex128 if precision == "exact" else np.complex64)
+        p = self.plan(ns, max_layers, max_bond, precision)
+        pinned = torch.from_numpy(host.view(np.float64 if precision == "exact" else np.float32)).pin_memory()
+        sv = p.vec()
         sv.copy_(pinned, non_blocking=True)
         return p, sv
 
@@ -209,14 +230,14 @@ class Engine:
         sp = self._sp(stream)
         tensors = torch.empty(max(p.tensor_elems, 1) * 2, dtype=torch.float64, device="cuda")
         bonds = torch.empty(p.B * (p.max_n + 1), dtype=torch.int32, device="cuda")
-        target = torch.empty_like(sv)
+        target = p.vec()
         self.hd.check(self.lib.qmprs_mps_from_statevector(p.p, _ptr(sv), int(bond_dimension), 1e-10,
                                                           _ptr(tensors), _ptr(bonds), _ptr(target), sp))
         return tensors, bonds, target
 
     def mps_to_statevector(self, p: Plan, tensors: torch.Tensor, bonds: torch.Tensor, stream=None) -> torch.Tensor:
         sp = self._sp(stream)
-        out = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        out = p.vec()
         self.hd.check(self.lib.qmprs_mps_to_statevector(p.p, _ptr(tensors), _ptr(bonds), _ptr(out), sp))
         return out
 
@@ -246,7 +267,7 @@ class Engine:
 
     def stage_circuit(self, p: Plan, gates, arity, nl, stream=None) -> torch.Tensor:
         sp = self._sp(stream)
-        circ = torch.empty(p.vec_elems * 2, dtype=torch.float32, device="cuda")
+        circ = p.vec()
         self.hd.check(self.lib.qmprs_circuit_state(p.p, _ptr(gates), _ptr(arity), _ptr(nl), _ptr(circ), sp))
         return circ
 
@@ -311,7 +332,7 @@ class Engine:
         return vec * torch.repeat_interleave(inv, counts)
 
     def encode_iterative(self, statevectors, bond_dimension: int, num_layers: int, sweeps_per_layer: int,
-                         nqubits=None, schedule: str = "iter_dioall") -> BatchResult:
+                         nqubits=None, schedule: str = "iter_dioall", precision: str = "fast") -> BatchResult:
         """Iterative schedules (arXiv:2209.00595, documented by the reference
         at qmprs/synthesis/mps_encoding/sequential.py:410-433): for k =
         1..num_layers, generate one analytic layer from the residual
@@ -328,9 +349,9 @@ class Engine:
             raise ValueError("schedule must be 'iter_dioall' or 'iter_dioi'.")
         dioi = schedule == "iter_dioi"
         if nqubits is None:
-            p, sv = self.upload(statevectors, num_layers, bond_dimension)
+            p, sv = self.upload(statevectors, num_layers, bond_dimension, precision)
         else:
-            p = self.plan(nqubits, num_layers, bond_dimension)
+            p = self.plan(nqubits, num_layers, bond_dimension, precision)
             sv = statevectors if statevectors.is_cuda else statevectors.to("cuda", non_blocking=True)
         _, _, target = self.stage_mps(p, sv, bond_dimension)
         B, L, S = p.B, int(num_layers), int(sweeps_per_layer)
@@ -408,17 +429,19 @@ class Engine:
         (``qmprs_plan_upload``: one cudaMalloc per plan, reused) on the
         current stream and return a tensor view of it.  The current stream
         first waits for the previous call's last use of that buffer."""
-        if host.dtype != torch.float32 or not host.is_contiguous():
-            raise ValueError("packed statevectors must be a contiguous float32 tensor")
+        if host.dtype != p.vdtype or not host.is_contiguous():
+            raise ValueError(f"packed statevectors must be a contiguous {p.vdtype} tensor")
         cur = torch.cuda.current_stream()
         ev = getattr(p, "input_free", None)
         if ev is not None:
             cur.wait_event(ev)
         dev = ctypes.c_void_p()
-        self.hd.check(self.lib.qmprs_plan_upload(p.p, ctypes.c_void_p(host.data_ptr()), host.numel() * 4,
+        self.hd.check(self.lib.qmprs_plan_upload(p.p, ctypes.c_void_p(host.data_ptr()),
+                                                 host.numel() * host.element_size(),
                                                  ctypes.c_void_p(cur.cuda_stream), ctypes.byref(dev)))
         p.input_ptr = dev.value
-        return torch.as_tensor(_DeviceBuffer(dev.value, host.numel()), device="cuda")
+        typestr = "<f8" if p.precision == "exact" else "<f4"
+        return torch.as_tensor(_DeviceBuffer(dev.value, host.numel(), typestr), device="cuda")
 
     @staticmethod
     def _release_input(p: Plan, sv: torch.Tensor) -> None:
@@ -430,7 +453,8 @@ class Engine:
     # ---- whole path ------------------------------------------------------------
     def encode(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
                fidelity_threshold: float = 1 - 1e-6, stop_fidelity: float = 0.0,
-               keep_tensors: bool = False, nqubits=None, download: bool = True, warm_start=None) -> BatchResult:
+               keep_tensors: bool = False, nqubits=None, download: bool = True, warm_start=None,
+               precision: str = "fast") -> BatchResult:
         """``prepare_state`` for a batch: (a) -> (b)+(c) -> (d) -> fidelity.
 
         ``statevectors`` is either a list of complex arrays, or (with
@@ -444,14 +468,19 @@ class Engine:
         ``stop_fidelity > 0`` every state that ends below it is swept again
         from its analytic layers (the plain method) and keeps the better of
         the two results.
+
+        ``precision="exact"`` runs the double-float mode
+        (``QMPRS_PRECISION_EXACT``): a packed buffer is then float64 pairs
+        (complex128), and the per-layer and per-sweep fidelities follow an
+        FP64 run of the reference's algorithm.
         """
         if nqubits is None:
-            p, sv = self.upload(statevectors, num_layers, bond_dimension)
+            p, sv = self.upload(statevectors, num_layers, bond_dimension, precision)
         else:
-            p = self.plan(nqubits, num_layers, bond_dimension)
+            p = self.plan(nqubits, num_layers, bond_dimension, precision)
             sv = statevectors
-            if sv.numel() != 2 * p.vec_elems:
-                raise ValueError("packed statevector buffer does not match the qubit counts")
+            if sv.numel() != 2 * p.vec_elems or sv.dtype != p.vdtype:
+                raise ValueError("packed statevector buffer does not match the qubit counts and precision")
             if not sv.is_cuda:
                 sv = self._stage_input(p, sv)
         tensors, bonds, target = self.stage_mps(p, sv, bond_dimension)

@@ -214,6 +214,8 @@ int qmprs_overlap(qmprs_plan_t p, const void* a, const void* b, void* out, void*
  * QMPRS_ERR_UNSUPPORTED.  The first call on a device looks up the scratch
  * address (make it before any stream capture); calls share the scratch, so
  * calls that overlap on the GPU race and must be serialised by the caller.
+ * A CUDA error already pending on the calling thread is left in place and
+ * the call returns QMPRS_ERR_CUDA without launching.
  * No counterpart in the reference (which has no device code).
  */
 #define QMPRS_NOALLOC_MAX_STATES 64

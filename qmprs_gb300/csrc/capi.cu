@@ -106,6 +106,8 @@ int check_kernel_errors(qmprs_plan* p, cudaStream_t s) {
   int flags = 0;
   CK(cudaMemcpyAsync(&flags, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (flags & KERR_BAD_INPUT)
+    return set_err(p->h, QMPRS_ERR_INVALID, "The statevector must have a finite, non-zero norm.");
   if (flags & KERR_NONUNITARY)
     return set_err(p->h, QMPRS_ERR_NONUNITARY, "All the generated unitaries must be unitary.");
   if (flags & KERR_EIG_WIDTH)
@@ -171,6 +173,11 @@ __global__ void k_fill_int(int* p, int64_t count, int value) {
     p[i] = value;
 }
 
+__global__ void k_check_norms(int B, const double2* sq, int* err) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x)
+    if (!(isfinite(sq[b].x) && sq[b].x > 0.0)) atomicOr(err, KERR_BAD_INPUT);
+}
+
 __global__ void k_count_active(int B, const int* active, int* num_active) {
   __shared__ int cnt;
   if (threadIdx.x == 0) cnt = 0;
@@ -188,6 +195,11 @@ void launch_fill_int(int* p, int64_t count, int value, cudaStream_t s) {
   if (blocks < 1) blocks = 1;
   qm_note_launch();
   k_fill_int<<<blocks, 256, 0, s>>>(p, count, value);
+}
+
+void launch_check_norms(int B, const double2* sq, int* err, cudaStream_t s) {
+  qm_note_launch();
+  k_check_norms<<<(B + 127) / 128, 128, 0, s>>>(B, sq, err);
 }
 
 void launch_count_active(int B, const int* active, int* num_active, cudaStream_t s) {
@@ -305,6 +317,7 @@ int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, d
   CK(cudaMemcpyAsync(bonds, p->d_bond_init, sizeof(int) * (size_t)p->B * stride, cudaMemcpyDeviceToDevice, s));
   launch_x_from_d(p->bd, sv, p->X0, s);
   launch_x_dot(p->bd, p->X0, p->X0, p->partials, p->sq, s);
+  launch_check_norms(p->B, p->sq, p->d_err, s);
   std::vector<double2> sq(p->B);
   CK(cudaMemcpyAsync(sq.data(), p->sq, sizeof(double2) * p->B, cudaMemcpyDeviceToHost, s));
   std::vector<int> hb((size_t)p->B * stride), start(p->B, -1);
@@ -747,6 +760,7 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
   const int64_t nb = (int64_t)p->B * (p->max_n + 1);
   CK(cudaMemcpyAsync(bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
   launch_overlap(p->bd, sv, sv, p->partials, p->sq, s);
+  launch_check_norms(p->B, p->sq, p->d_err, s);
   float2* buf[2] = {p->S0, p->S1};
   const int stride = p->max_n + 1;
   std::vector<int> hb(wide ? (size_t)p->B * stride : 0);

@@ -55,6 +55,7 @@ enum {
   KERR_NONFINITE = 4,
   KERR_BAD_GATE = 8,
   KERR_TC_TIMEOUT = 16,   // a tensor-core completion wait ran out
+  KERR_BAD_INPUT = 32,    // an input statevector has a non-finite or zero norm
 };
 
 struct BatchDev {
@@ -198,6 +199,8 @@ void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, c
 void qm_note_launch();   // counts every kernel launch the library issues
 void launch_fill_int(int* p, int64_t count, int value, cudaStream_t s);
 void launch_count_active(int B, const int* active, int* num_active, cudaStream_t s);
+// raise KERR_BAD_INPUT unless every sq[b].x is finite and positive
+void launch_check_norms(int B, const double2* sq, int* err, cudaStream_t s);
 
 #define TT_SPLIT 8
 

@@ -16,7 +16,9 @@
 // it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
+#include <mutex>
 
 #include "device_common.cuh"
 #include "qmprs_gb300.h"
@@ -87,8 +89,10 @@ __global__ void k_noalloc_reduce(NoallocLayout L, const double2* scratch, double
 
 // Device address of the scratch array, looked up once per device with that
 // device current (the array's host-side name is not a device address).
-static double2* g_noalloc_ptr[64];
-static bool g_noalloc_ready[64];
+// Threads that call at the same time on a fresh device serialise on the
+// lookup; the published address is read with acquire ordering.
+static std::atomic<double2*> g_noalloc_ptr[64];
+static std::mutex g_noalloc_mu;
 
 extern "C" int qmprs_overlap_noalloc(const void* a, const void* b, int num_states, const int* num_qubits,
                                      void* out, void* stream) {
@@ -110,20 +114,27 @@ extern "C" int qmprs_overlap_noalloc(const void* a, const void* b, int num_state
     if (tiles > QMPRS_NOALLOC_MAX_TILES) return QMPRS_ERR_UNSUPPORTED;
   }
   L.ntiles = tiles;
+  // An error left pending by earlier work on this thread belongs to its
+  // caller: refuse to launch and leave it in place rather than report it
+  // as ours (or clear it).
+  if (cudaPeekAtLastError() != cudaSuccess) return QMPRS_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return QMPRS_ERR_CUDA;
-  if (!g_noalloc_ready[dev]) {
-    double2* ptr = nullptr;
-    if (cudaGetSymbolAddress((void**)&ptr, g_noalloc_partials) != cudaSuccess || ptr == nullptr)
-      return QMPRS_ERR_CUDA;
-    g_noalloc_ptr[dev] = ptr;
-    g_noalloc_ready[dev] = true;
+  double2* scratch = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    scratch = g_noalloc_ptr[dev].load(std::memory_order_relaxed);
+    if (!scratch) {
+      if (cudaGetSymbolAddress((void**)&scratch, g_noalloc_partials) != cudaSuccess || scratch == nullptr)
+        return QMPRS_ERR_CUDA;
+      g_noalloc_ptr[dev].store(scratch, std::memory_order_release);
+    }
   }
-  double2* scratch = g_noalloc_ptr[dev];
   cudaStream_t s = (cudaStream_t)stream;
   const int grid = tiles < 152 * 8 ? tiles : 152 * 8;
   qm_note_launch();
   k_noalloc_overlap<<<grid, BLOCK_THREADS, 0, s>>>(L, (const float2*)a, (const float2*)b, scratch);
+  if (cudaGetLastError() != cudaSuccess) return QMPRS_ERR_CUDA;   // the reduce is not queued
   qm_note_launch();
   k_noalloc_reduce<<<(num_states + 7) / 8, 256, 0, s>>>(L, scratch, (double2*)out);
   return cudaGetLastError() == cudaSuccess ? QMPRS_OK : QMPRS_ERR_CUDA;

@@ -15,9 +15,14 @@ import numpy as np
 
 class Ket:
     def __init__(self, data, normalize: bool = True) -> None:
+        rows = None
         if isinstance(data, Ket):
+            rows = data.rows
             data = data.data
-        v = np.asarray(data, dtype=np.complex128).reshape(-1)
+        arr = np.asarray(data, dtype=np.complex128)
+        if arr.ndim == 2:
+            rows = arr.shape[0]      # an image: snake indexing walks its rows
+        v = arr.reshape(-1)
         if v.size == 0:
             raise ValueError("a statevector needs at least one amplitude")
         n = max(1, int(np.ceil(np.log2(v.size))))
@@ -31,15 +36,18 @@ class Ket:
                 v = v / nrm
         self.data = v
         self.num_qubits = n
+        # rows of the 2-D view used by snake indexing (the input's own rows
+        # for a 2-D array whose size is a power of two)
+        self.rows = rows if rows and v.size % rows == 0 and arr.size == v.size else 2 ** ((n + 1) // 2)
 
     def change_indexing(self, index_type: str) -> None:
         """``"row"`` keeps the amplitude order; ``"snake"`` reverses every odd
-        row of the amplitudes viewed as a 2^ceil(n/2) x 2^floor(n/2) image."""
+        row of the amplitudes viewed as an image: the input's own rows for a
+        2-D input, else 2^ceil(n/2) x 2^floor(n/2)."""
         if index_type == "row":
             return
         if index_type == "snake":
-            rows = 2 ** ((self.num_qubits + 1) // 2)
-            img = self.data.reshape(rows, -1).copy()
+            img = self.data.reshape(self.rows, -1).copy()
             img[1::2] = img[1::2, ::-1]
             self.data = img.reshape(-1)
             return

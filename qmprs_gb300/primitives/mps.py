@@ -35,7 +35,7 @@ from ..ket import Ket
 UnitaryBlock: TypeAlias = tuple
 UnitaryLayer: TypeAlias = list
 
-_MAX_SVD_BOND = 32   # largest bond the round-trip through kernel (a) supports (2 * bond <= 64)
+_MAX_SVD_BOND = 1024   # largest bond of the GPU statevector -> MPS stage
 
 
 class Tensor:
@@ -50,21 +50,35 @@ class Tensor:
 
 
 def _quimb_like(obj) -> bool:
-    """A quimb ``MatrixProductState``: site ``arrays`` and the index order
+    """A quimb ``MatrixProductState``: site ``arrays`` plus either
+    ``permute_arrays`` (quimb's own method, which reorders every site's
+    indices to a given order such as "lpr") or an index-order string
     ``shape`` (a permutation of "lrp")."""
+    if not hasattr(obj, "arrays"):
+        return False
+    if callable(getattr(obj, "permute_arrays", None)):
+        return True
     shape = getattr(obj, "shape", None)
-    return hasattr(obj, "arrays") and isinstance(shape, str) and sorted(shape) == ["l", "p", "r"]
+    return isinstance(shape, str) and sorted(shape) == ["l", "p", "r"]
 
 
 def _from_quimb(obj) -> "MatrixProductState":
-    """Site arrays of a quimb MPS in any index order, as (l, p, r) tensors.
-    The first site has no l index and the last no r index (quimb's open
-    boundary arrays)."""
+    """Site arrays of a quimb MPS as (l, p, r) tensors.  A quimb object is
+    copied and brought to index order "lpr" with its own
+    ``permute_arrays``, so its stored order never has to be known; an
+    object without that method states its order in ``shape``.  The first
+    site has no l index and the last no r index (quimb's open boundary
+    arrays)."""
+    order = getattr(obj, "shape", None)
+    if callable(getattr(obj, "permute_arrays", None)):
+        obj = obj.copy() if callable(getattr(obj, "copy", None)) else obj
+        obj.permute_arrays("lpr")
+        order = "lpr"
     arrays = [np.asarray(a) for a in obj.arrays]
     n = len(arrays)
     out = []
     for i, a in enumerate(arrays):
-        letters = obj.shape
+        letters = order
         if n > 1 and i == 0:
             letters = letters.replace("l", "")
         if n > 1 and i == n - 1:
@@ -72,7 +86,7 @@ def _from_quimb(obj) -> "MatrixProductState":
         if n == 1:
             letters = "p"
         if a.ndim != len(letters):
-            raise ValueError(f"site {i}: array of rank {a.ndim} does not match the index order {obj.shape!r}")
+            raise ValueError(f"site {i}: array of rank {a.ndim} does not match the index order {order!r}")
         want = "".join(c for c in "lpr" if c in letters)
         out.append(np.transpose(a, [letters.index(c) for c in want]))
     return MatrixProductState(out, layout="lpr")
@@ -176,6 +190,9 @@ class MPS:
             self.statevector = statevector
             self._tensors, self._dense = self._from_statevector_dev(statevector, bond_dimension)
             self._form = "right"
+            # the complex128 input, for encoders run in the exact precision
+            # mode (dropped once the state is changed)
+            self._exact_source = statevector.data
         elif (mps is not None) and (statevector is None):
             if not isinstance(mps, MatrixProductState) and _quimb_like(mps):
                 mps = _from_quimb(mps)
@@ -220,14 +237,17 @@ class MPS:
         return res.mps_tensors(0), target
 
     @staticmethod
-    def _dense_from_tensors(tensors) -> torch.Tensor:
+    def _dense_from_tensors(tensors, precision: str = "fast") -> torch.Tensor:
+        """Dense statevector of site tensors (l, p, r) on the GPU: complex64
+        (float32 pairs), or complex128 contracted in double-float with
+        ``precision="exact"``."""
         n = len(tensors)
         bonds = [1] + [int(t.shape[2]) for t in tensors[:-1]] + [1]
         chi = max(bonds)
         if chi > 1024:
             raise ValueError("MPS bonds above 1024 are not supported on the GPU path")
         eng = _engine.engine()
-        p = eng.plan([n], 1, chi)
+        p = eng.plan([n], 1, chi, precision)
         ce = p.chi_eff(0)
         store = np.zeros(p.tensor_elems, dtype=np.complex128)
         for s, t in enumerate(tensors):
@@ -246,6 +266,7 @@ class MPS:
         return self._dense.cpu().numpy().view(np.complex64).astype(np.complex128)
 
     def _set_dense(self, dense: torch.Tensor, form: str | None) -> None:
+        self._exact_source = None
         self._dense = dense
         self._tensors = None
         self._form = form
@@ -253,7 +274,15 @@ class MPS:
     def _recompute_tensors(self, max_bond: int | None, cutoff_form: str) -> None:
         """Site tensors of the dense state by the truncated SVD (right or left form)."""
         n = self.num_sites
-        chi = min(int(max_bond) if max_bond else _MAX_SVD_BOND, 2 ** (n // 2))
+        self._exact_source = None
+        if max_bond:
+            chi = min(int(max_bond), 2 ** (n // 2))
+            if chi > _MAX_SVD_BOND:
+                raise ValueError(f"bond dimensions above {_MAX_SVD_BOND} are not supported on the GPU path")
+        else:
+            # no max_bond: only quimb's cutoff truncates (reference
+            # qmprs/primitives/mps.py:441-453), so every bond may reach 2^(n/2)
+            chi = min(2 ** (n // 2), _MAX_SVD_BOND)
         vec = self._dense_np()
         if cutoff_form == "left":
             vec = vec.reshape([2] * n).transpose(list(range(n))[::-1]).reshape(-1)
@@ -268,6 +297,8 @@ class MPS:
                                   tensor_off=p.tensor_off, bonds=bonds.cpu().numpy(),
                                   max_n=p.max_n, max_bond=max(chi, 1))
         ts = res.mps_tensors(0)
+        if not max_bond and 2 ** (n // 2) > _MAX_SVD_BOND and max(t.shape[2] for t in ts[:-1]) >= _MAX_SVD_BOND:
+            raise ValueError(f"the state needs bonds above {_MAX_SVD_BOND}, which the GPU path does not support")
         if cutoff_form == "left":
             ts = [t.transpose(2, 1, 0).copy() for t in ts[::-1]]
             tvec = target.cpu().numpy().view(np.complex64).reshape([2] * n)

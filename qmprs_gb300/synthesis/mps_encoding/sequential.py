@@ -139,17 +139,49 @@ class Sequential(MPSEncoder):
         }
         return self._circuit_from_unitary_layers(mps, res.layers(0))
 
+    def _exact_unitary_circuit(self, mps: MPS, num_layers: int, num_sweeps: int):
+        """The same path in the exact precision mode (double-float working
+        states): from the MPS's complex128 input when it was built from a
+        statevector and not changed since, else from its site tensors
+        contracted in double-float."""
+        eng = _engine.engine()
+        n = mps.num_sites
+        sv = getattr(mps, "_exact_source", None)
+        if sv is not None:
+            chi = max(mps.bond_dimension, 1)
+        else:
+            ts = mps.mps.tensors3d()
+            chi = max([1] + [int(t.shape[2]) for t in ts[:-1]])
+            sv = MPS._dense_from_tensors(ts, "exact").cpu().numpy().view(np.complex128)
+        res = eng.encode([sv], chi, num_layers, num_sweeps, self.fidelity_threshold, precision="exact")
+        L = int(res.num_layers[0])
+        self.last_run = {
+            "layer_fidelities": res.layer_fidelities[0, :L],
+            "sweep_fidelities": res.sweep_fidelities[0] if num_sweeps > 0 else None,
+            "num_layers": L,
+        }
+        return self._circuit_from_unitary_layers(mps, res.layers(0))
+
     def prepare_mps(self, mps: MPS, **kwargs):
+        """``Sequential.prepare_mps`` (sequential.py:588-600).  Extension:
+        ``precision="exact"`` runs the double-float mode, whose per-layer and
+        per-sweep fidelities follow an FP64 run of the reference's algorithm
+        (the default "fast" keeps complex64 states)."""
         num_layers = kwargs.get("num_layers", 1)
         num_sweeps = kwargs.get("num_sweeps", 0)
+        precision = kwargs.get("precision", "fast")
         if not isinstance(num_layers, int) or num_layers < 1:
             raise ValueError("The number of layers must be a positive integer.")
+        if precision not in ("fast", "exact"):
+            raise ValueError("precision must be 'fast' or 'exact'.")
+        if precision == "exact":
+            return self._exact_unitary_circuit(mps, num_layers, num_sweeps)
         return self._sequential_unitary_circuit(mps, num_layers, num_sweeps)
 
     # ---- batched extension -------------------------------------------------------------
     def prepare_states(self, statevectors, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
                        stop_fidelity: float = 0.0, emit: bool = True, nqubits=None, *, warm_start=None,
-                       schedule: str = "oall"):
+                       schedule: str = "oall", precision: str = "fast"):
         """Encode many statevectors at once (any mix of qubit counts).
 
         Same result per state as ``prepare_state`` (default
@@ -163,6 +195,8 @@ class Sequential(MPSEncoder):
         ``warm_start`` (keyword only; a ``qmprs_gb300.warmstart.WarmStartMLP``)
         starts the sweeps from the network's predicted layers; states that
         end below ``stop_fidelity`` fall back to the analytic layers.
+        ``precision`` (keyword only): ``"fast"`` or ``"exact"`` (double-float
+        working states; a packed buffer is then float64 pairs).
         ``schedule`` (keyword only): ``"oall"`` (the reference's: all layers,
         then ``num_sweeps`` sweeps), ``"iter_dioall"`` (one layer at a time
         from the residual, each followed by ``num_sweeps`` sweeps of all
@@ -172,6 +206,8 @@ class Sequential(MPSEncoder):
         """
         if schedule not in ("oall", "iter_dioall", "iter_dioi"):
             raise ValueError("schedule must be 'oall', 'iter_dioall' or 'iter_dioi'.")
+        if precision not in ("fast", "exact"):
+            raise ValueError("precision must be 'fast' or 'exact'.")
         if not isinstance(num_layers, int) or num_layers < 1:
             raise ValueError("The number of layers must be a positive integer.")
         if not isinstance(bond_dimension, int) or bond_dimension < 1:
@@ -183,10 +219,10 @@ class Sequential(MPSEncoder):
                 raise ValueError("The statevector must have at least 2 qubits.")
             if schedule != "oall":
                 res = eng.encode_iterative(statevectors, bond_dimension, num_layers, num_sweeps, nqubits=ns,
-                                           schedule=schedule)
+                                           schedule=schedule, precision=precision)
             else:
                 res = eng.encode(statevectors, bond_dimension, num_layers, num_sweeps, self.fidelity_threshold,
-                                 stop_fidelity, nqubits=ns, warm_start=warm_start)
+                                 stop_fidelity, nqubits=ns, warm_start=warm_start, precision=precision)
         else:
             kets = [sv if isinstance(sv, Ket) else Ket(sv) for sv in statevectors]
             ns = [k.num_qubits for k in kets]
@@ -194,10 +230,10 @@ class Sequential(MPSEncoder):
                 raise ValueError("The statevector must have at least 2 qubits.")
             if schedule != "oall":
                 res = eng.encode_iterative([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
-                                           schedule=schedule)
+                                           schedule=schedule, precision=precision)
             else:
                 res = eng.encode([k.data for k in kets], bond_dimension, num_layers, num_sweeps,
-                                 self.fidelity_threshold, stop_fidelity, warm_start=warm_start)
+                                 self.fidelity_threshold, stop_fidelity, warm_start=warm_start, precision=precision)
         circuits = None
         if emit:
             circuits = []

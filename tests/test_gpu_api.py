@@ -167,3 +167,57 @@ def test_packed_host_input_matches_device(api):
         assert np.array_equal(rh.fidelity, rd.fidelity)
     with pytest.raises(ValueError):
         Sequential(Circuit).prepare_states(host[:-2], nqubits=ns, emit=False, **cfg)
+
+
+@pytest.mark.parametrize("n", [12, 14])
+def test_compress_without_max_bond_truncates_only_at_the_cutoff(api, n):
+    """compress() with no max_bond truncates only at quimb's cutoff
+    (reference qmprs/primitives/mps.py:441-453): a random state keeps its
+    full bonds (128 at 14 qubits) and the site tensors match the oracle's
+    right-canonical ones."""
+    MPS, _, _ = api
+    sv = S.uniform_complex(n, 4)
+    m = MPS(statevector=sv, bond_dimension=512)
+    m.compress()
+    got = m.mps.tensors3d()
+    sv64 = sv.astype(np.complex64).astype(np.complex128)
+    ref = D.tt_svd_right(sv64 / np.linalg.norm(sv64), n, 2 ** (n // 2))
+    assert max(t.shape[2] for t in got[:-1]) == 2 ** (n // 2)
+    for s in range(n):
+        assert got[s].shape == ref[s].shape, s
+        assert np.max(np.abs(got[s] - ref[s])) < 2e-4, s
+
+
+def test_prepare_state_applies_snake_indexing_and_compression(api):
+    """prepare_state(index_type="snake", compression_percentage=p)
+    (reference qmprs/synthesis/mps_encoding/base.py:96-102) encodes the
+    re-indexed, compressed state: the same circuit as encoding that state
+    directly, and a better fit to it than to the raw input."""
+    from qmprs_gb300.ket import Ket
+    _, Sequential, Circuit = api
+    img = S.uniform_complex(8, 21).reshape(16, 16)
+    enc = Sequential(Circuit)
+    c1 = enc.prepare_state(img, 64, compression_percentage=30.0, index_type="snake", num_layers=3, num_sweeps=2)
+    k = Ket(img)
+    k.change_indexing("snake")
+    k.compress(30.0)
+    c2 = enc.prepare_state(k.data, 64, num_layers=3, num_sweeps=2)
+    assert np.allclose(c1.get_statevector(), c2.get_statevector(), atol=1e-6)
+    raw = img.reshape(-1) / np.linalg.norm(img)
+    assert _fid(c1, k.data) > _fid(c1, raw)
+
+
+def test_packed_input_with_non_finite_amplitudes_is_rejected(api):
+    """The packed batch path skips the statevector wrapper's validation;
+    stage (a) checks every state's norm on the device instead."""
+    import torch
+    _, Sequential, Circuit = api
+    good = S.uniform_complex(6, 3).astype(np.complex64)
+    bad = S.uniform_complex(7, 4).astype(np.complex64)
+    bad[5] = np.nan
+    packed = torch.from_numpy(np.concatenate([good, bad]).view(np.float32).copy())
+    with pytest.raises(ValueError, match="finite"):
+        Sequential(Circuit).prepare_states(packed, 16, num_layers=1, nqubits=[6, 7])
+    zero = torch.zeros(2 * 2 ** 6, dtype=torch.float32)
+    with pytest.raises(ValueError, match="finite"):
+        Sequential(Circuit).prepare_states(zero, 16, num_layers=1, nqubits=[6])

@@ -185,3 +185,20 @@ def test_fast_mode_error_on_benchmark_sample(eng):
         worst = max(worst, dl, ds)
     print(f"fast mode on the benchmark sample: max difference {worst:.2e}")
     assert worst < 1e-4
+
+
+def test_prepare_state_exact_precision_through_the_reference_api(cuda_lib):
+    """``Sequential.prepare_state(..., precision="exact")``: the reference's
+    entry point (qmprs/synthesis/mps_encoding/base.py:58-106) with the
+    double-float mode; per-layer and per-sweep fidelities (``last_run``) and
+    the emitted circuit's state against the FP64 oracle."""
+    from qmprs_gb300.circuit import Circuit
+    from qmprs_gb300.synthesis.mps_encoding import Sequential
+    sv = S.uniform_complex(9, 5)
+    enc = Sequential(Circuit)
+    c = enc.prepare_state(sv, 32, num_layers=8, num_sweeps=6, precision="exact")
+    _, lf, sf, fid = _oracle(sv, 32, 8, 6)
+    assert len(enc.last_run["layer_fidelities"]) == len(lf)
+    assert np.max(np.abs(enc.last_run["layer_fidelities"] - lf)) < FID_TOL
+    assert np.max(np.abs(enc.last_run["sweep_fidelities"] - sf)) < FID_TOL
+    assert abs(abs(np.vdot(c.get_statevector(), sv)) - fid) < 1e-5

@@ -215,8 +215,13 @@ def get_unitary_layers(mps: Mps, num_layers: int, threshold: float = 1 - 1e-6,
 
 
 def prepare_state(statevector, bond_dimension: int, num_layers: int = 1, num_sweeps: int = 0,
-                  threshold: float = 1 - 1e-6, conv: str = "literal") -> D.EncodeResult:
-    """The reference path end to end on an explicit MPS (CPU proxy of the reference)."""
+                  threshold: float = 1 - 1e-6, conv: str = "literal",
+                  stop_fidelity: float = 0.0) -> D.EncodeResult:
+    """The reference path end to end on an explicit MPS (CPU proxy of the reference).
+
+    ``stop_fidelity > 0`` ends the sweeps once a sweep's fidelity with the
+    target reaches it (the per-state stop of the batched GPU path; the
+    reference itself always runs ``num_sweeps``)."""
     sv = D.ket(statevector)
     n = D.num_qubits(sv)
     if n < 2:
@@ -228,6 +233,8 @@ def prepare_state(statevector, bond_dimension: int, num_layers: int = 1, num_swe
     for _ in range(num_sweeps):
         layers, f = D.sweep(target, n, layers, conv)
         sf.append(f)
+        if stop_fidelity > 0.0 and f >= stop_fidelity:
+            break
     psi = D.circuit_state(layers, n)
     fid = float(abs(np.vdot(psi, sv)))
     return D.EncodeResult(layers=layers, layer_fidelities=lf, sweep_fidelities=sf, target=target, fidelity=fid)

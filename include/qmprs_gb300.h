@@ -115,6 +115,26 @@ int qmprs_plan_set_precision(qmprs_plan_t p, int precision);
 int qmprs_plan_precision(qmprs_plan_t p);
 
 /*
+ * CUDA graphs of the layer stage (qmprs_unitary_layers) and the sweep stage
+ * (qmprs_optimize_layers), on by default.  A stage's launch sequence is
+ * fixed by its arguments (buffer addresses, sizes, layer and sweep counts,
+ * thresholds) and, for the sweeps, by the group counts of the gates it is
+ * given.  The first call with a given set runs launch by launch; the second
+ * records the stage on a stream private to the plan and replays it as one
+ * graph on the caller's stream, and later calls replay it.  In a graph every
+ * layer and sweep is enqueued without host synchronisation: states that
+ * reach the early-exit or stop fidelity are skipped on the device, so the
+ * results are bit-identical to the launch-by-launch path, which stops at
+ * the first layer or sweep after which no state is left.  A plan keeps at
+ * most 16 graphs (oldest dropped first).  qmprs_plan_graph_stats returns
+ * the graphs cached and the replays so far.
+ * Replaces: the reference's per-layer and per-sweep Python loops
+ * (qmprs/synthesis/mps_encoding/sequential.py:384-391, 532-539).
+ */
+int qmprs_plan_set_graphs(qmprs_plan_t p, int enable);
+int qmprs_plan_graph_stats(qmprs_plan_t p, int* cached, int64_t* replays);
+
+/*
  * Copy a packed complex64 statevector batch (`bytes` = vec_elems * 8, from
  * host memory, ideally pinned) into the plan's own device input buffer on
  * `stream` and return that buffer in *dev_out, ready for

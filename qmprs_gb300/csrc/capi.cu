@@ -67,6 +67,17 @@ struct qmprs_plan {
   // exact precision mode: double-float working states (allocated on first use)
   int precision = QMPRS_PRECISION_FAST;
   xc *X0 = nullptr, *X1 = nullptr, *X2 = nullptr, *XT = nullptr;
+  // CUDA graphs of the layer and sweep stages, keyed by everything their
+  // launches embed (see run_stage)
+  bool graphs = true;
+  cudaStream_t cap = nullptr;
+  int64_t graph_replays = 0;
+  struct Graph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+  };
+  std::vector<Graph> graph_cache;
 };
 
 static std::atomic<long long> g_launches{0};
@@ -235,6 +246,70 @@ void launch_wide_contract(qmprs_plan* p, int step, const double2* tensors, const
 
 namespace {
 
+// Enqueue a stage whose launch sequence is fixed by `key` (pointers, sizes,
+// options) through body(stream, capturing).  Without graphs body runs on the
+// caller's stream.  With graphs: the first call with a key runs body
+// directly; the second captures body on the plan's own capture stream (a
+// stream the caller never sees, so nothing of the caller's work is
+// captured), instantiates the graph and launches it on the caller's
+// stream; later calls launch the cached graph.  A capturing body must not
+// synchronise: it enqueues every sweep or layer and leaves converged states
+// to the kernels' device-side active flags.  Kernel launches replayed from
+// a graph are added to the launch counter at every replay.
+template <class F>
+int run_stage(qmprs_plan* p, const std::vector<uint64_t>& key, cudaStream_t s, F&& body) {
+  if (!p->graphs || p->prof) return body(s, false);
+  qmprs_plan::Graph* e = nullptr;
+  for (auto& g : p->graph_cache)
+    if (g.key == key) e = &g;
+  if (e && e->exec) {
+    CK(cudaGraphLaunch(e->exec, s));
+    g_launches.fetch_add(e->launches, std::memory_order_relaxed);
+    ++p->graph_replays;
+    return QMPRS_OK;
+  }
+  if (!e) {
+    if (p->graph_cache.size() >= 16) {   // bound the cache: drop the oldest graph
+      if (p->graph_cache.front().exec) cudaGraphExecDestroy(p->graph_cache.front().exec);
+      p->graph_cache.erase(p->graph_cache.begin());
+    }
+    p->graph_cache.push_back(qmprs_plan::Graph{key, nullptr, 0});
+    return body(s, false);
+  }
+  if (!p->cap) CK(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+  const long long before = g_launches.load();
+  CK(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+  const int rc = body(p->cap, true);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(p->cap, &graph);
+  const long long n = g_launches.load() - before;
+  g_launches.fetch_sub(n, std::memory_order_relaxed);
+  if (rc != QMPRS_OK || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    if (rc != QMPRS_OK) return rc;
+    return cuda_fail(p->h, ce, "stage graph capture");
+  }
+  const cudaError_t ie = cudaGraphInstantiate(&e->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    e->exec = nullptr;
+    return cuda_fail(p->h, ie, "cudaGraphInstantiate");
+  }
+  e->launches = n;
+  CK(cudaGraphLaunch(e->exec, s));
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  ++p->graph_replays;
+  return QMPRS_OK;
+}
+
+inline uint64_t ptr_key(const void* q) { return (uint64_t)(uintptr_t)q; }
+inline uint64_t dbl_key(double v) {
+  uint64_t u;
+  std::memcpy(&u, &v, sizeof(u));
+  return u;
+}
+
 int ensure_tt_scratch(qmprs_plan* p) {
   if (p->tt_partials) return QMPRS_OK;
   const int64_t WW = (int64_t)p->tt_w * p->tt_w;
@@ -389,26 +464,35 @@ int exact_unitary_layers(qmprs_plan* p, const double2* target, int num_layers, d
   xc* buf[2] = {p->X1, p->X2};
   const double atol = 1.0 - fidelity_threshold;
   const int64_t nb = (int64_t)p->B * (p->max_n + 1);
-  for (int l = 0; l < num_layers; ++l) {
-    CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
-    for (int j = 0; j + 2 <= p->max_n; ++j) {
-      const xc* src = j == 0 ? work : buf[(j - 1) & 1];
-      launch_x_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->active, s);
-      launch_layer_eig(p->bd, j, p->partials, p->vsel, p->bonds, p->site_t, p->active, s);
-      launch_x_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s);
+  auto body = [&](cudaStream_t s2, bool capturing) -> int {
+    for (int l = 0; l < num_layers; ++l) {
+      CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s2));
+      for (int j = 0; j + 2 <= p->max_n; ++j) {
+        const xc* src = j == 0 ? work : buf[(j - 1) & 1];
+        launch_x_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->active, s2);
+        launch_layer_eig(p->bd, j, p->partials, p->vsel, p->bonds, p->site_t, p->active, s2);
+        launch_x_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s2);
+      }
+      launch_x_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s2);
+      for (int st = 0; st < p->max_n; ++st) {
+        GateSel sel{SEL_INVERSE, st, l, 1, gates, ar, nullptr, p->active};
+        launch_x_apply_gate(p->bd, work, sel, s2);
+      }
+      launch_x_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s2);
+      if (!capturing) {
+        launch_count_active(p->B, p->active, p->num_active, s2);
+        int na = 0;
+        CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s2));
+        CK(cudaStreamSynchronize(s2));
+        if (na == 0) break;
+      }
     }
-    launch_x_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s);
-    for (int st = 0; st < p->max_n; ++st) {
-      GateSel sel{SEL_INVERSE, st, l, 1, gates, ar, nullptr, p->active};
-      launch_x_apply_gate(p->bd, work, sel, s);
-    }
-    launch_x_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
-    launch_count_active(p->B, p->active, p->num_active, s);
-    int na = 0;
-    CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (na == 0) break;
-  }
+    return QMPRS_OK;
+  };
+  const std::vector<uint64_t> key = {3, ptr_key(target), ptr_key(gates), ptr_key(ar), ptr_key(layers_out),
+                                     ptr_key(layer_fid), (uint64_t)num_layers, dbl_key(fidelity_threshold)};
+  rc = run_stage(p, key, s, body);
+  if (rc != QMPRS_OK) return rc;
   return check_kernel_errors(p, s);
 }
 
@@ -424,28 +508,36 @@ int exact_optimize_layers(qmprs_plan* p, const double2* target, double2* gates, 
   launch_x_dot(p->bd, p->XT, p->XT, p->partials, p->tnorm, s);
   xc* psi = p->X0;
   xc* t = p->X1;
-  for (int sw = 0; sw < num_sweeps; ++sw) {
-    launch_x_zero(p->bd, psi, p->active, s);
-    for (int j = 0; j < max_gates; ++j) {
-      GateSel sel{SEL_REBUILD, j, 0, 0, gates, ar, num_layers, p->active};
-      launch_x_apply_gate(p->bd, psi, sel, s);
+  auto body = [&](cudaStream_t s2, bool capturing) -> int {
+    for (int sw = 0; sw < num_sweeps; ++sw) {
+      launch_x_zero(p->bd, psi, p->active, s2);
+      for (int j = 0; j < max_gates; ++j) {
+        GateSel sel{SEL_REBUILD, j, 0, 0, gates, ar, num_layers, p->active};
+        launch_x_apply_gate(p->bd, psi, sel, s2);
+      }
+      launch_x_copy(p->bd, p->XT, t, p->active, s2);
+      for (int j = 0; j < max_gates; ++j) {
+        launch_x_sweep_step(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, p->nuc, s2);
+        GateSel sel{SEL_SWEEP, j, 0, 1, gates, ar, num_layers, p->active};
+        launch_x_apply_gate(p->bd, t, sel, s2);
+      }
+      CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s2));
+      launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active,
+                          stop_fidelity, p->num_active, s2);
+      if (stop_fidelity > 0.0 && !capturing) {
+        int na = 0;
+        CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s2));
+        CK(cudaStreamSynchronize(s2));
+        if (na == 0) break;
+      }
     }
-    launch_x_copy(p->bd, p->XT, t, p->active, s);
-    for (int j = 0; j < max_gates; ++j) {
-      launch_x_sweep_step(p->bd, j, psi, t, gates, ar, num_layers, p->active, p->partials, p->nuc, s);
-      GateSel sel{SEL_SWEEP, j, 0, 1, gates, ar, num_layers, p->active};
-      launch_x_apply_gate(p->bd, t, sel, s);
-    }
-    CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));
-    launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active, stop_fidelity,
-                        p->num_active, s);
-    if (stop_fidelity > 0.0) {
-      int na = 0;
-      CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      if (na == 0) break;
-    }
-  }
+    return QMPRS_OK;
+  };
+  const std::vector<uint64_t> key = {4, ptr_key(target), ptr_key(gates), ptr_key(ar), ptr_key(num_layers),
+                                     ptr_key(sweep_fid), ptr_key(sweeps_done), (uint64_t)num_sweeps,
+                                     dbl_key(stop_fidelity), (uint64_t)max_gates};
+  rc = run_stage(p, key, s, body);
+  if (rc != QMPRS_OK) return rc;
   return check_kernel_errors(p, s);
 }
 
@@ -510,6 +602,9 @@ const char* qmprs_last_error(qmprs_handle_t h) { return h ? h->err.c_str() : "nu
 
 void qmprs_plan_destroy(qmprs_plan_t p) {
   if (!p) return;
+  for (auto& g : p->graph_cache)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (p->cap) cudaStreamDestroy(p->cap);
   void* ptrs[] = {p->d_n,      p->d_tile_state, p->d_tile_idx, p->d_state_tile0, p->d_state_ntiles,
                   p->d_ticket, p->d_err,        p->d_vec_off,  p->d_gate_off,    p->d_tensor_off,
                   p->d_bond_init, p->S0,        p->S1,         p->S2,            p->partials,
@@ -714,6 +809,21 @@ int qmprs_plan_set_precision(qmprs_plan_t p, int precision) {
 
 int qmprs_plan_precision(qmprs_plan_t p) { return p ? p->precision : -1; }
 
+int qmprs_plan_set_graphs(qmprs_plan_t p, int enable) {
+  if (!p) return QMPRS_ERR_INVALID;
+  p->graphs = enable != 0;
+  return QMPRS_OK;
+}
+
+int qmprs_plan_graph_stats(qmprs_plan_t p, int* cached, int64_t* replays) {
+  if (!p) return QMPRS_ERR_INVALID;
+  int c = 0;
+  for (auto& g : p->graph_cache) c += g.exec != nullptr;
+  if (cached) *cached = c;
+  if (replays) *replays = p->graph_replays;
+  return QMPRS_OK;
+}
+
 int qmprs_plan_upload(qmprs_plan_t p, const void* host, int64_t bytes, void* stream, void** dev_out) {
   if (!p || !host || !dev_out) return QMPRS_ERR_INVALID;
   *dev_out = nullptr;
@@ -879,28 +989,38 @@ int qmprs_unitary_layers(qmprs_plan_t p, const void* target_, int num_layers, do
   float2* buf[2] = {p->S1, p->S2};
   const double atol = 1.0 - fidelity_threshold;
   const int64_t nb = (int64_t)p->B * (p->max_n + 1);
-  for (int l = 0; l < num_layers; ++l) {
-    CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, s));
-    for (int j = 0; j + 2 <= p->max_n; ++j) {
-      const float2* src = j == 0 ? work : buf[(j - 1) & 1];
-      launch_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->vsel, p->bonds, p->site_t, p->active, s);
-      launch_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, s);
+  auto body = [&](cudaStream_t st, bool capturing) -> int {
+    for (int l = 0; l < num_layers; ++l) {
+      CK(cudaMemcpyAsync(p->bonds, p->d_bond_init, sizeof(int) * nb, cudaMemcpyDeviceToDevice, st));
+      for (int j = 0; j + 2 <= p->max_n; ++j) {
+        const float2* src = j == 0 ? work : buf[(j - 1) & 1];
+        launch_layer_gram(p->bd, j, work, src, p->bonds, p->partials, p->vsel, p->bonds, p->site_t, p->active,
+                          st);
+        launch_layer_project(p->bd, j, work, src, buf[j & 1], p->bonds, p->vsel, p->active, st);
+      }
+      launch_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, st);
+      // inverse of the new layer: tile passes of two 4-qubit windows (up to
+      // six gates per read and write of the working state)
+      launch_layer_plan(p->bd, p->gd, ar, ORDER_LAYER_INV, l, p->active, st);
+      for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
+        // exact FP32 products: the next layer's bond-2 truncation decides at
+        // singular values near the 1e-10 cutoff of this working state
+        launch_rebuild_pass(p->bd, p->gd, r, work, gates, ar, nullptr, p->active, st, ORDER_LAYER_INV, l, true);
+      launch_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, st);
+      if (!capturing) {
+        launch_count_active(p->B, p->active, p->num_active, st);
+        int na = 0;
+        CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (na == 0) break;
+      }
     }
-    launch_layer_build(p->bd, l, buf[0], buf[1], p->bonds, p->site_t, gates, ar, p->active, s);
-    // inverse of the new layer: tile passes of two 4-qubit windows (up to
-    // six gates per read and write of the working state)
-    launch_layer_plan(p->bd, p->gd, ar, ORDER_LAYER_INV, l, p->active, s);
-    for (int r = 0; r < layer_pass_bound(p->max_n); ++r)
-      // exact FP32 products: the next layer's bond-2 truncation decides at
-      // singular values near the 1e-10 cutoff of this working state
-      launch_rebuild_pass(p->bd, p->gd, r, work, gates, ar, nullptr, p->active, s, ORDER_LAYER_INV, l, true);
-    launch_layer_fidelity(p->bd, l, work, num_layers, atol, layer_fid, layers_out, p->active, s);
-    launch_count_active(p->B, p->active, p->num_active, s);
-    int na = 0;
-    CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (na == 0) break;
-  }
+    return QMPRS_OK;
+  };
+  const std::vector<uint64_t> key = {2, ptr_key(target), ptr_key(gates), ptr_key(ar), ptr_key(layers_out),
+                                     ptr_key(layer_fid), (uint64_t)num_layers, dbl_key(fidelity_threshold)};
+  const int rc = run_stage(p, key, s, body);
+  if (rc != QMPRS_OK) return rc;
   return check_kernel_errors(p, s);
 }
 
@@ -939,55 +1059,63 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   }
   float2* psi = p->S0;
   float2* t = p->S1;
-  ProfLog log;
   const bool prof = p->prof;
-  std::vector<int> act(p->B, 1);
-  for (int sw = 0; sw < num_sweeps; ++sw) {
-    // algorithmic bytes per rebuild pass / group pass, counted from the
-    // states active in this sweep
-    std::vector<double> amp_rb(prof ? max_rpasses : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
-    if (prof) {
-      CK(cudaMemcpyAsync(act.data(), p->active, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      for (int b = 0; b < p->B; ++b)
-        if (act[b]) {
-          for (int r = 0; r < (nrgroups[b] + 1) / 2; ++r) amp_rb[r] += (double)ipow2(p->n[b]);
-          for (int g = 0; g < ngroups[b]; ++g) amp_grp[g] += (double)ipow2(p->n[b]);
-        }
+  auto body = [&](cudaStream_t st, bool capturing) -> int {
+    ProfLog log;
+    std::vector<int> act(p->B, 1);
+    for (int sw = 0; sw < num_sweeps; ++sw) {
+      // algorithmic bytes per rebuild pass / group pass, counted from the
+      // states active in this sweep
+      std::vector<double> amp_rb(prof ? max_rpasses : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
+      if (prof) {
+        CK(cudaMemcpyAsync(act.data(), p->active, sizeof(int) * p->B, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int b = 0; b < p->B; ++b)
+          if (act[b]) {
+            for (int r = 0; r < (nrgroups[b] + 1) / 2; ++r) amp_rb[r] += (double)ipow2(p->n[b]);
+            for (int g = 0; g < ngroups[b]; ++g) amp_grp[g] += (double)ipow2(p->n[b]);
+          }
+      }
+      // C|0>: two 4-qubit windows of consecutive gates per pass
+      launch_set_zero_state(p->bd, psi, p->active, st);
+      for (int r = 0; r < max_rpasses; ++r) {
+        log.begin(prof, st);
+        launch_rebuild_pass(p->bd, p->gd, r, psi, gates, ar, num_layers, p->active, st);
+        log.end(prof, 2, st);
+        if (prof) p->prof_bytes[2] += 16.0 * amp_rb[r];
+      }
+      // backward sweep by groups: the pass applies group g-1's peels to psi
+      // and its new gates to t (the target itself for g = 1) and reduces the
+      // cross matrix of group g; the polar kernel runs group g's steps on it
+      for (int g = 0; g < max_groups; ++g) {
+        log.begin(prof, st);
+        const int e = launch_group_pass(p->bd, p->gd, g, psi, g <= 1 ? target : t, t, gates, ar, num_layers,
+                                        p->active, p->tnorm, st);
+        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "cudaFuncSetAttribute(k_group_pass)");
+        log.end(prof, 0, st);
+        log.begin(prof, st);
+        launch_group_polar(p->bd, p->gd, g, gates, ar, num_layers, p->active, p->nuc, st);
+        log.end(prof, 3, st);
+        if (prof) p->prof_bytes[0] += (g == 0 ? 16.0 : 32.0) * amp_grp[g];
+      }
+      log.flush(p);
+      CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), st));
+      launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active,
+                          stop_fidelity, p->num_active, st);
+      if (stop_fidelity > 0.0 && !capturing) {
+        int na = 0;
+        CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (na == 0) break;
+      }
     }
-    // C|0>: two 4-qubit windows of consecutive gates per pass
-    launch_set_zero_state(p->bd, psi, p->active, s);
-    for (int r = 0; r < max_rpasses; ++r) {
-      log.begin(prof, s);
-      launch_rebuild_pass(p->bd, p->gd, r, psi, gates, ar, num_layers, p->active, s);
-      log.end(prof, 2, s);
-      if (prof) p->prof_bytes[2] += 16.0 * amp_rb[r];
-    }
-    // backward sweep by groups: the pass applies group g-1's peels to psi
-    // and its new gates to t (the target itself for g = 1) and reduces the
-    // cross matrix of group g; the polar kernel runs group g's steps on it
-    for (int g = 0; g < max_groups; ++g) {
-      log.begin(prof, s);
-      const int e = launch_group_pass(p->bd, p->gd, g, psi, g <= 1 ? target : t, t, gates, ar, num_layers,
-                                      p->active, p->tnorm, s);
-      if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "cudaFuncSetAttribute(k_group_pass)");
-      log.end(prof, 0, s);
-      log.begin(prof, s);
-      launch_group_polar(p->bd, p->gd, g, gates, ar, num_layers, p->active, p->nuc, s);
-      log.end(prof, 3, s);
-      if (prof) p->prof_bytes[0] += (g == 0 ? 16.0 : 32.0) * amp_grp[g];
-    }
-    log.flush(p);
-    CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), s));
-    launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active, stop_fidelity,
-                        p->num_active, s);
-    if (stop_fidelity > 0.0) {
-      int na = 0;
-      CK(cudaMemcpyAsync(&na, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      if (na == 0) break;
-    }
-  }
+    return QMPRS_OK;
+  };
+  const std::vector<uint64_t> key = {1, ptr_key(target), ptr_key(gates), ptr_key(ar), ptr_key(num_layers),
+                                     ptr_key(sweep_fid), ptr_key(sweeps_done), (uint64_t)num_sweeps,
+                                     dbl_key(stop_fidelity), (uint64_t)max_groups, (uint64_t)max_rpasses};
+  rc = run_stage(p, key, s, body);
+  if (rc != QMPRS_OK) return rc;
   return check_kernel_errors(p, s);
 }
 

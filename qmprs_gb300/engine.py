@@ -282,6 +282,17 @@ class Engine:
         self.hd.check(self.lib.qmprs_apply_layer(p.p, _ptr(vec), _ptr(gates), _ptr(arity), int(layer),
                                                  1 if inverse else 0, sp))
 
+    def set_graphs(self, p: Plan, on: bool) -> None:
+        """Replay the layer and sweep stages of plan ``p`` as CUDA graphs (the
+        default) or launch them one by one."""
+        self.hd.check(self.lib.qmprs_plan_set_graphs(p.p, 1 if on else 0))
+
+    def graph_stats(self, p: Plan) -> tuple[int, int]:
+        """(graphs cached, graph replays so far) of plan ``p``."""
+        c, r = ctypes.c_int(), ctypes.c_int64()
+        self.hd.check(self.lib.qmprs_plan_graph_stats(p.p, ctypes.byref(c), ctypes.byref(r)))
+        return c.value, r.value
+
     def set_profiling(self, p: Plan, on: bool) -> None:
         self.hd.check(self.lib.qmprs_plan_set_profiling(p.p, 1 if on else 0))
 

@@ -135,6 +135,26 @@ int qmprs_plan_set_graphs(qmprs_plan_t p, int enable);
 int qmprs_plan_graph_stats(qmprs_plan_t p, int* cached, int64_t* replays);
 
 /*
+ * Autotuner of the sweep's tile passes (on by default).  The grouped sweep
+ * and the circuit rebuild run grid-stride loops over chunks of 32 tiles of
+ * 2^11 amplitudes; how many blocks take them decides how evenly states of
+ * uneven size and group count spread over the 152 SMs.  On a batch whose
+ * signature (qubit-count histogram, bond dimension, layer count) the handle
+ * has not seen, the first sweeps of qmprs_optimize_layers each run one
+ * candidate grid (4 blocks per SM, the resident maximum; one block per
+ * chunk, balanced by the hardware scheduler; 2 blocks per SM), timed with
+ * events and divided by the states active in that sweep; the fastest is
+ * used for the rest of the call, by the layer stage's passes, and by every
+ * later plan with the same signature on the handle.  The grid changes no
+ * result (each chunk is reduced in a fixed order whichever block takes
+ * it).  qmprs_plan_tuning returns the grid in use and whether it came from
+ * the autotuner.
+ * Replaces: nothing in the reference (its sweep runs one state on the CPU).
+ */
+int qmprs_plan_set_autotune(qmprs_plan_t p, int enable);
+int qmprs_plan_tuning(qmprs_plan_t p, int* pass_grid, int* tuned);
+
+/*
  * Copy a packed complex64 statevector batch (`bytes` = vec_elems * 8, from
  * host memory, ideally pinned) into the plan's own device input buffer on
  * `stream` and return that buffer in *dev_out, ready for

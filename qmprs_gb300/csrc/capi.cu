@@ -20,6 +20,8 @@
 struct qmprs_ctx {
   int device = 0;
   std::string err;
+  // autotuned tile-pass grids, by batch signature (see plan_signature)
+  std::vector<std::pair<uint64_t, int>> tuned;
 };
 
 struct qmprs_plan {
@@ -72,6 +74,8 @@ struct qmprs_plan {
   bool graphs = true;
   cudaStream_t cap = nullptr;
   int64_t graph_replays = 0;
+  bool autotune = true;
+  bool tuned = false;
   struct Graph {
     std::vector<uint64_t> key;
     cudaGraphExec_t exec = nullptr;
@@ -304,6 +308,24 @@ int run_stage(qmprs_plan* p, const std::vector<uint64_t>& key, cudaStream_t s, F
 }
 
 inline uint64_t ptr_key(const void* q) { return (uint64_t)(uintptr_t)q; }
+
+// Signature of a batch for the autotuner: the qubit-count histogram, the
+// bond dimension and the layer count (FNV-1a).
+uint64_t plan_signature(const qmprs_plan* p) {
+  int hist[MAX_QUBITS + 1] = {0};
+  for (int n : p->n) ++hist[n];
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xff;
+      h *= 1099511628211ull;
+    }
+  };
+  for (int n = 0; n <= MAX_QUBITS; ++n) mix((uint64_t)hist[n]);
+  mix((uint64_t)p->max_bond);
+  mix((uint64_t)p->max_layers);
+  return h;
+}
 inline uint64_t dbl_key(double v) {
   uint64_t u;
   std::memcpy(&u, &v, sizeof(u));
@@ -762,6 +784,7 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   gd.old_gates = p->d_old_gates;
   gd.partials = p->d_gpartials;
   gd.rgrp = p->d_rgrp;
+  gd.grid = 0;
   gd.nrgroups = p->d_nrgroups;
   BatchDev& bd = p->bd;
   bd.B = B;
@@ -808,6 +831,20 @@ int qmprs_plan_set_precision(qmprs_plan_t p, int precision) {
 }
 
 int qmprs_plan_precision(qmprs_plan_t p) { return p ? p->precision : -1; }
+
+int qmprs_plan_set_autotune(qmprs_plan_t p, int enable) {
+  if (!p) return QMPRS_ERR_INVALID;
+  p->autotune = enable != 0;
+  if (!p->autotune) p->gd.grid = 0;
+  return QMPRS_OK;
+}
+
+int qmprs_plan_tuning(qmprs_plan_t p, int* pass_grid, int* tuned) {
+  if (!p) return QMPRS_ERR_INVALID;
+  if (pass_grid) *pass_grid = p->gd.grid > 0 ? std::min(p->gd.grid, p->nchunks) : std::min(PASS_GRID_DEFAULT, p->nchunks);
+  if (tuned) *tuned = p->tuned ? 1 : 0;
+  return QMPRS_OK;
+}
 
 int qmprs_plan_set_graphs(qmprs_plan_t p, int enable) {
   if (!p) return QMPRS_ERR_INVALID;
@@ -1060,10 +1097,45 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   float2* psi = p->S0;
   float2* t = p->S1;
   const bool prof = p->prof;
+  // Autotuner of the tile passes' grid: on a batch signature the handle has
+  // not tuned yet, the first sweeps run one candidate each (the resident
+  // blocks, 4 per SM; one block per chunk, scheduled by the hardware; 2 per
+  // SM), timed with events over the sweep and divided by the states active
+  // in it; the fastest is kept for the rest of the call and cached on the
+  // handle.  The grid changes no result: every chunk is reduced in a fixed
+  // order whichever block takes it.
+  const uint64_t sig = plan_signature(p);
+  bool tune = false;
+  if (p->autotune && !prof) {
+    bool found = false;
+    for (auto& e : p->h->tuned)
+      if (e.first == sig) {
+        p->gd.grid = e.second;
+        found = true;
+      }
+    tune = !found && num_sweeps >= 2;
+    p->tuned = found;
+  }
+  const std::vector<int> cands = {PASS_GRID_DEFAULT, p->nchunks, 2 * 152};
   auto body = [&](cudaStream_t st, bool capturing) -> int {
     ProfLog log;
     std::vector<int> act(p->B, 1);
+    std::vector<double> cost;
+    cudaEvent_t te[2] = {nullptr, nullptr};
+    if (tune) {
+      CK(cudaEventCreate(&te[0]));
+      CK(cudaEventCreate(&te[1]));
+    }
     for (int sw = 0; sw < num_sweeps; ++sw) {
+      const bool trial = tune && sw < (int)cands.size();
+      int nact = 0;
+      if (trial) {
+        p->gd.grid = cands[sw];
+        launch_count_active(p->B, p->active, p->num_active, st);
+        CK(cudaMemcpyAsync(&nact, p->num_active, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(cudaEventRecord(te[0], st));
+      }
       // algorithmic bytes per rebuild pass / group pass, counted from the
       // states active in this sweep
       std::vector<double> amp_rb(prof ? max_rpasses : 0, 0.0), amp_grp(prof ? max_groups : 0, 0.0);
@@ -1099,6 +1171,19 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
         if (prof) p->prof_bytes[0] += (g == 0 ? 16.0 : 32.0) * amp_grp[g];
       }
       log.flush(p);
+      if (trial) {
+        CK(cudaEventRecord(te[1], st));
+        CK(cudaEventSynchronize(te[1]));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, te[0], te[1]));
+        cost.push_back(nact > 0 ? ms / nact : 1e30);
+        if (sw + 1 == (int)cands.size() || sw + 1 == num_sweeps) {
+          const int best = (int)(std::min_element(cost.begin(), cost.end()) - cost.begin());
+          p->gd.grid = cands[best];
+          p->h->tuned.push_back({sig, cands[best]});
+          p->tuned = true;
+        }
+      }
       CK(cudaMemsetAsync(p->num_active, 0, sizeof(int), st));
       launch_sweep_finish(p->B, sw, num_sweeps, p->nuc, p->tnorm, sweep_fid, sweeps_done, p->active,
                           stop_fidelity, p->num_active, st);
@@ -1109,12 +1194,21 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
         if (na == 0) break;
       }
     }
+    if (tune && !p->tuned && !cost.empty()) {   // the call ended before every candidate ran
+      const int best = (int)(std::min_element(cost.begin(), cost.end()) - cost.begin());
+      p->gd.grid = cands[best];
+      p->h->tuned.push_back({sig, cands[best]});
+      p->tuned = true;
+    }
+    for (cudaEvent_t e : te)
+      if (e) cudaEventDestroy(e);
     return QMPRS_OK;
   };
   const std::vector<uint64_t> key = {1, ptr_key(target), ptr_key(gates), ptr_key(ar), ptr_key(num_layers),
                                      ptr_key(sweep_fid), ptr_key(sweeps_done), (uint64_t)num_sweeps,
-                                     dbl_key(stop_fidelity), (uint64_t)max_groups, (uint64_t)max_rpasses};
-  rc = run_stage(p, key, s, body);
+                                     dbl_key(stop_fidelity), (uint64_t)max_groups, (uint64_t)max_rpasses,
+                                     (uint64_t)p->gd.grid};
+  rc = tune ? body(s, false) : run_stage(p, key, s, body);
   if (rc != QMPRS_OK) return rc;
   return check_kernel_errors(p, s);
 }

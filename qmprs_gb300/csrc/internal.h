@@ -105,6 +105,7 @@ struct GateSel {
 #define GT 11
 #define GCHUNK 32
 #define GMAXSTEPS 8
+#define PASS_GRID_DEFAULT (4 * 152)   // resident blocks of the tile passes (4 per SM)
 
 struct GroupEnt {
   int j0;     // first backward step
@@ -126,6 +127,7 @@ struct GroupDev {
   double2* partials;         // [nchunks * GMM]
   GroupEnt* rgrp;            // [B * gmax] forward-order groups (circuit rebuild)
   int* nrgroups;             // [B]
+  int grid;                  // blocks of the tile-pass launches (0: min(nchunks, 4 per SM)); set by the autotuner
 };
 
 // ---- launches (defined in the .cu files) ---------------------------------

@@ -1067,6 +1067,14 @@ void launch_layer_plan(const BatchDev& bd, const GroupDev& gd, const signed char
   k_group_plan<<<blocks, 128, 0, s>>>(bd, gd, arity, nullptr, mode, layer, active, gd.rgrp, gd.nrgroups);
 }
 
+// Blocks of a tile-pass launch: the autotuned count, or at most the
+// resident blocks (PASS_BLOCKS_PER_SM per SM); never more than the chunks.
+static int pass_grid(const GroupDev& gd) {
+  int grid = gd.grid > 0 ? gd.grid : PASS_BLOCKS_PER_SM * 152;
+  if (grid > gd.nchunks) grid = gd.nchunks;
+  return grid < 1 ? 1 : grid;
+}
+
 int layer_pass_bound(int max_n) {
   // a group covers at least three new sites of the layer, except the last
   const int groups = (max_n + 2) / 3 + 1;
@@ -1076,8 +1084,7 @@ int layer_pass_bound(int max_n) {
 void launch_rebuild_pass(const BatchDev& bd, const GroupDev& gd, int pass, float2* psi, const double2* gates,
                          const signed char* arity, const int* nlayers, const int* active, cudaStream_t s, int mode,
                          int layer, bool exact) {
-  int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
-  if (grid < 1) grid = 1;
+  int grid = pass_grid(gd);
   qm_note_launch();
   k_rebuild_pass<<<grid, PASS_THREADS, (size_t)2 * sizeof(float2) << GT, s>>>(bd, gd, pass, psi, gates, arity,
                                                                           nlayers, active, mode, layer, exact);
@@ -1093,8 +1100,7 @@ int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi
     if (e != cudaSuccess) return (int)e;
     attr_set = true;
   }
-  int grid = gd.nchunks < PASS_BLOCKS_PER_SM * 152 ? gd.nchunks : PASS_BLOCKS_PER_SM * 152;
-  if (grid < 1) grid = 1;
+  int grid = pass_grid(gd);
   qm_note_launch();
   k_group_pass<<<grid, PASS_THREADS, PASS_DYN_SMEM, s>>>(bd, gd, g, psi, z_in, z_out, gates, gd.old_gates, arity,
                                                           nlayers, active, znorm);

@@ -287,6 +287,16 @@ class Engine:
         default) or launch them one by one."""
         self.hd.check(self.lib.qmprs_plan_set_graphs(p.p, 1 if on else 0))
 
+    def set_autotune(self, p: Plan, on: bool) -> None:
+        """Let the sweep stage pick the tile passes' grid by timing (the default)."""
+        self.hd.check(self.lib.qmprs_plan_set_autotune(p.p, 1 if on else 0))
+
+    def tuning(self, p: Plan) -> tuple[int, bool]:
+        """(grid of the tile passes, chosen by the autotuner) of plan ``p``."""
+        g, t = ctypes.c_int(), ctypes.c_int()
+        self.hd.check(self.lib.qmprs_plan_tuning(p.p, ctypes.byref(g), ctypes.byref(t)))
+        return g.value, bool(t.value)
+
     def graph_stats(self, p: Plan) -> tuple[int, int]:
         """(graphs cached, graph replays so far) of plan ``p``."""
         c, r = ctypes.c_int(), ctypes.c_int64()

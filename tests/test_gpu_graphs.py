@@ -50,3 +50,35 @@ def test_graph_replay_is_bit_identical(eng, precision, stop):
         for a, b in zip(_fields(r), _fields(ref)):
             assert np.array_equal(a, b)
     assert int(ref.num_layers[2]) < 5                         # the product state left the layer stage early
+
+
+def test_autotuned_grid_changes_no_result(eng):
+    """The sweep's autotuner (qmprs_plan_set_autotune) times candidate grids
+    of the tile passes on the first sweeps (here 384 chunks: 384, 384 and
+    304 blocks); its choice changes no bit of the result, and it is cached
+    on the handle for later plans of the same batch signature."""
+    import torch
+    from qmprs_gb300 import engine as E
+    ns = [21] * 12
+    svs = [S.random_mps(21, 4, 40 + i) for i in range(12)]
+    kw = dict(num_layers=2, num_sweeps=4)
+    p = eng.plan(ns, 2, 16)
+    eng.set_autotune(p, False)
+    eng.set_graphs(p, False)
+    ref = eng.encode(svs, 16, **kw)
+    assert eng.tuning(p) == (384, False)
+    eng.set_autotune(p, True)
+    runs = [eng.encode(svs, 16, **kw) for _ in range(2)]
+    grid, tuned = eng.tuning(p)
+    assert tuned and grid in (384, 304)
+    for r in runs:
+        for a, b in zip(_fields(r), _fields(ref)):
+            assert np.array_equal(a, b)
+    q = E.Plan(eng.hd, ns, 2, 16)                  # a second plan of the same signature
+    assert eng.tuning(q) == (384, False)
+    packed = np.concatenate([v.astype(np.complex64) for v in svs])
+    sv = torch.from_numpy(packed.view(np.float32).copy()).cuda()
+    _, _, target = eng.stage_mps(q, sv, 16)
+    gates, arity, nl, _ = eng.stage_layers(q, target, 2, 1 - 1e-6)
+    eng.stage_sweeps(q, target, gates, arity, nl, 1, 0.0)
+    assert eng.tuning(q) == (grid, True)

@@ -15,9 +15,9 @@
 // which keeps about 2^-46 of relative precision on the FP32 pipes.  The
 // small algebra is FP64: the eigensolvers of stage (a) and of the layer
 // cuts (shared with the fast mode), the closed-form gate construction, and
-// the sweep's polar factor (FP64 one-sided Jacobi; the fast mode's FP32
-// variant is accurate to ~1e-7, which rank-deficient environments carry
-// into later steps at first order).
+// the sweep's polar factor (FP64 one-sided Jacobi, started from FP32
+// sweeps; the fast mode's FP32 polar is accurate to ~1e-7, which
+// rank-deficient environments carry into later steps at first order).
 //
 // Caller-facing statevector buffers of this mode are complex128; the plan
 // converts them to double-float scratch on entry and back on exit.
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_x_sweep_step(BatchDev bd, int
           // directions that follow the current gate, and an FP32 completion
           // of them would enter the later steps at first order
           for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
-          const double nn = polar_jacobi(ee, m, w, wprev);
+          const double nn = polar_jacobi_pre(ee, m, w, wprev);
           for (int i = 0; i < m * m; ++i) gptr[i] = cconj(w[i]);
           nuc[b] = nn;
         }

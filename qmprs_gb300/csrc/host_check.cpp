@@ -24,6 +24,16 @@ double hc_polar(const double* e, int m, double* w_out, const double* w_prev) {
   return nuc;
 }
 
+double hc_polar_pre(const double* e, int m, double* w_out, const double* w_prev) {
+  double2 a[16], w[16], wp[16];
+  for (int i = 0; i < m * m; ++i) a[i] = cd(e[2 * i], e[2 * i + 1]);
+  if (w_prev)
+    for (int i = 0; i < m * m; ++i) wp[i] = cd(w_prev[2 * i], w_prev[2 * i + 1]);
+  double nuc = polar_jacobi_pre(a, m, w, w_prev ? wp : nullptr);
+  for (int i = 0; i < m * m; ++i) { w_out[2 * i] = w[i].x; w_out[2 * i + 1] = w[i].y; }
+  return nuc;
+}
+
 double hc_polar_sweep(const double* e, int m, double* w_out, const double* w_prev) {
   double2 a[16], w[16], wp[16];
   for (int i = 0; i < m * m; ++i) a[i] = cd(e[2 * i], e[2 * i + 1]);

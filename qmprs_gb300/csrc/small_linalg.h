@@ -365,6 +365,12 @@ QM_HD QM_NOINLINE void polar_null_part(const double2 (&u)[M][M], const double2 (
                                        const double2* w_prev, double2* w_out);
 
 template <int M>
+QM_HD void jacobi_precondition(double2 (&a)[M][M], double2 (&vv)[M][M]);
+
+// PRE: start the FP64 sweeps from FP32 ones (jacobi_precondition); the
+// FP64 sweeps then converge in one or two rounds instead of six to eight,
+// with the same stopping rule and the same result to FP64 rounding.
+template <int M, bool PRE = false>
 QM_HD double polar_jacobi_m(const double2* e, double2* w_out, const double2* w_prev) {
   double2 a[M][M], vv[M][M];
 #pragma unroll
@@ -374,6 +380,7 @@ QM_HD double polar_jacobi_m(const double2* e, double2* w_out, const double2* w_p
       a[c][r] = e[r * M + c];
       vv[c][r] = cd(r == c ? 1.0 : 0.0, 0.0);
     }
+  if constexpr (PRE) jacobi_precondition<M>(a, vv);
   jacobi_sweeps<M>(a, vv, (1 << M) - 1);
   double sig[M], smax = 0.0, nuc = 0.0;
 #pragma unroll
@@ -556,6 +563,72 @@ QM_HD void jacobi_sweeps_f(float2 (&a)[M][M], float2 (&v)[M][M], int mask) {
         if (((mask >> p) & 1) && ((mask >> q) & 1)) rotated |= jacobi_pair_f<M>(a, v, p, q);
     if (!rotated) break;
   }
+}
+
+// Preconditioner of the FP64 one-sided Jacobi: FP32 Hestenes sweeps on a
+// float copy of the columns of a (scaled by a power of two) give V0 to
+// FP32 accuracy; V0 is made unitary in FP64 (modified Gram-Schmidt, twice)
+// and a <- a V0, vv <- V0, so the FP64 sweeps that follow start from
+// nearly orthogonal columns.  GB300's FP64 units run a single thread's
+// dependent chain at about 31 ns per operation, FP32 at about 2 ns.
+template <int M>
+QM_HD void jacobi_precondition(double2 (&a)[M][M], double2 (&vv)[M][M]) {
+  double amax = 0.0;
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) amax = fmax(amax, fmax(fabs(a[c][r].x), fabs(a[c][r].y)));
+  if (!(amax > 0.0) || !isfinite(amax)) return;
+  int ex = 0;
+  frexp(amax, &ex);
+  float2 a32[M][M], v32[M][M];
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      a32[c][r] = cf((float)ldexp(a[c][r].x, -ex), (float)ldexp(a[c][r].y, -ex));
+      v32[c][r] = cf(r == c ? 1.f : 0.f, 0.f);
+    }
+  jacobi_sweeps_f<M>(a32, v32, (1 << M) - 1);
+  double2 v[M][M];
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+#pragma unroll
+    for (int r = 0; r < M; ++r) v[c][r] = f2d(v32[c][r]);
+    for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+      for (int o = 0; o < c; ++o) {
+        double2 d = czero();
+#pragma unroll
+        for (int r = 0; r < M; ++r) d = cadd(d, cmulc(v[o][r], v[c][r]));
+#pragma unroll
+        for (int r = 0; r < M; ++r) v[c][r] = csub(v[c][r], cmul(v[o][r], d));
+      }
+      double nrm = 0.0;
+#pragma unroll
+      for (int r = 0; r < M; ++r) nrm += cnorm2(v[c][r]);
+      const double in = 1.0 / sqrt(nrm);
+#pragma unroll
+      for (int r = 0; r < M; ++r) v[c][r] = cscale(v[c][r], in);
+    }
+  }
+  double2 av[M][M];   // (A V0) column c = sum_k a[k] V0[k][c]
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      double2 acc = czero();
+#pragma unroll
+      for (int k = 0; k < M; ++k) acc = cadd(acc, cmul(a[k][r], v[c][k]));
+      av[c][r] = acc;
+    }
+#pragma unroll
+  for (int c = 0; c < M; ++c)
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+      a[c][r] = av[c][r];
+      vv[c][r] = v[c][r];
+    }
 }
 
 template <int M>
@@ -909,6 +982,12 @@ QM_HD void ran_gate_single(const double2* v2, double2* g) {
 // Polar factor dispatch (m in {2, 4}).
 QM_HD double polar_jacobi(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
   return m == 4 ? polar_jacobi_m<4>(e, w_out, w_prev) : polar_jacobi_m<2>(e, w_out, w_prev);
+}
+
+// FP64 polar factor (polar_jacobi) started from FP32 sweeps: the exact
+// mode's sweep update.
+QM_HD double polar_jacobi_pre(const double2* e, int m, double2* w_out, const double2* w_prev = nullptr) {
+  return m == 4 ? polar_jacobi_m<4, true>(e, w_out, w_prev) : polar_jacobi_m<2, true>(e, w_out, w_prev);
 }
 
 // Polar factor used by the sweep kernel (FP32 sweeps, FP64 finish).

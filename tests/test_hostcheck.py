@@ -22,6 +22,8 @@ def hc():
     lib.hc_herm_eig.argtypes = [dp, ctypes.c_int, dp, dp]
     lib.hc_polar.argtypes = [dp, ctypes.c_int, dp, dp]
     lib.hc_polar.restype = ctypes.c_double
+    lib.hc_polar_pre.argtypes = [dp, ctypes.c_int, dp, dp]
+    lib.hc_polar_pre.restype = ctypes.c_double
     lib.hc_polar_sweep.argtypes = [dp, ctypes.c_int, dp, dp]
     lib.hc_polar_sweep.restype = ctypes.c_double
     lib.hc_complement.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
@@ -313,3 +315,45 @@ def test_tensor_core_scale_keeps_fp16_in_range(hc):
             assert nrm * s <= 2.0 ** 15
             if n // 2 + 4 <= 15:
                 assert 4.0 <= nrm * 2.0 ** (-n / 2) * s <= 32.0
+
+
+@pytest.mark.parametrize("m", [2, 4])
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("cond", [1.0, 1e-3, 1e-5])
+def test_preconditioned_polar_is_the_fp64_polar(hc, m, seed, cond):
+    """The exact mode's polar (FP32 Hestenes sweeps, then the FP64 sweeps of
+    polar_jacobi from there) gives the FP64 polar factor and nuclear norm,
+    also for ill-conditioned environments."""
+    rng = np.random.default_rng(300 + seed)
+    u, _ = np.linalg.qr(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    v, _ = np.linalg.qr(rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    s = np.geomspace(1.0, cond, m)
+    e = _c((u * s) @ v.conj().T * 0.37)
+    w = np.zeros((m, m), np.complex128)
+    nuc = hc.hc_polar_pre(_p(e), m, _p(w), None)
+    wref, sref = cv.polar_unitary(e)
+    assert np.allclose(w, wref, atol=1e-11 / cond)
+    assert abs(nuc - sref.sum()) < 1e-12
+    w64 = np.zeros((m, m), np.complex128)
+    hc.hc_polar(_p(e), m, _p(w64), None)
+    assert np.allclose(w, w64, atol=1e-11 / cond)
+
+
+@pytest.mark.parametrize("rank", [0, 1, 2, 3])
+@pytest.mark.parametrize("seed", range(3))
+def test_preconditioned_polar_null_space_follows_previous(hc, rank, seed):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((4, rank)) + 1j * rng.standard_normal((4, rank))
+    b = rng.standard_normal((rank, 4)) + 1j * rng.standard_normal((rank, 4))
+    e = _c(a @ b)
+    e = e + 1e-9 * (rng.standard_normal((4, 4)))
+    prev, _ = np.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    prev = _c(prev)
+    w = np.zeros((4, 4), np.complex128)
+    hc.hc_polar_pre(_p(_c(e)), 4, _p(w), _p(prev))
+    ref, _ = cv.polar_unitary_canonical(e, prev)
+    assert np.allclose(w.conj().T @ w, np.eye(4), atol=1e-10)
+    assert np.allclose(w, ref, atol=1e-7)
+    w64 = np.zeros((4, 4), np.complex128)
+    hc.hc_polar(_p(_c(e)), 4, _p(w64), _p(prev))
+    assert np.allclose(w, w64, atol=1e-9)

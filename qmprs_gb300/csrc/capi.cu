@@ -432,7 +432,8 @@ int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, d
                     p->gram + (int64_t)b * WW, s);
       wide = wide || 2 * r > TT_MAXW;
     }
-    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond, s);
+    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond,
+                  p->tt_partials, 1e-15, s);
     if (wide) {
       for (int b = 0; b < p->B; ++b) {
         const int c = p->n[b] - 1 - j;
@@ -919,7 +920,8 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
   for (int j = 0; j + 2 <= p->max_n; ++j) {
     const float2* src = j == 0 ? sv : buf[(j - 1) & 1];
     launch_tt_gram(p->bd, j, sv, src, bonds, p->tt_partials, p->gram, s);
-    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond, s);
+    launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond,
+                  p->tt_partials, 1e-13, s);
     launch_tt_project(p->bd, j, sv, src, buf[j & 1], bonds, p->vsel2, s);
     // Grams wider than 128 and projections to more than 64 columns: the
     // device-wide path, state by state (possible only after 6 cuts)

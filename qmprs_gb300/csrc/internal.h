@@ -182,7 +182,8 @@ void launch_sweep_finish(int B, int sweep, int num_sweeps, const double* nuc, co
 void launch_tt_gram(const BatchDev& bd, int step, const float2* sv, const float2* src, const int* bonds,
                     double2* partials, double2* gram, cudaStream_t s);
 void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, double2* vwork, int max_bond,
-                   double cutoff, double2* vsel, double2* tensors, int chi, cudaStream_t s);
+                   double cutoff, double2* vsel, double2* tensors, int chi, double2* scratch, double fine,
+                   cudaStream_t s);
 void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const float2* src, float2* dst,
                        const int* bonds, const double2* vsel, cudaStream_t s);
 void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1, const int* bonds,

@@ -295,17 +295,21 @@ __device__ void smem_matmul(const double2* A, const double2* B, double2* Cm, int
 // Jacobi round is four block-wide phases, and shared memory takes the
 // memory latency out of them.
 //
-// In shared memory the eigenvectors are found in two precisions.  FP32
-// Jacobi sweeps on a float copy of G converge V to FP32 accuracy at the
-// FP32 rate; V is then made orthonormal in FP64 by one Newton-Schulz step
-// V <- V (3I - V^H V) / 2 (its FP32 error of about 1e-7 leaves about 1e-14),
-// G is replaced by the similar, nearly diagonal V^H G V, and the FP64
-// Jacobi sweeps finish from there, accumulating into the same V.  On the
+// The eigenvectors are found in two precisions.  FP32 Jacobi sweeps on a
+// float copy of G converge V to FP32 accuracy at the FP32 rate; V is then
+// made orthonormal in FP64 by one Newton-Schulz step V <- V (3I - V^H V) / 2
+// (its FP32 error of about 1e-7 leaves about 1e-14), G is replaced by the
+// similar, nearly diagonal V^H G V, and the FP64 Jacobi sweeps finish from
+// there, accumulating into the same V, down to `fine` of the trace.  On the
 // Grams of the benchmark family this cuts the FP64 rotations from about 8.4
-// sweeps' worth to about 2.2 (w = 64).
+// sweeps' worth to about 2.2 (w = 64).  For 64 < w <= 128 the same steps
+// run in global memory (L2 resident): the float copies in `scratch32` (the
+// Gram partials, already reduced) and the FP64 scratch in the state's slot
+// of `vsel` (written only at the end).
 __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step, int* bonds, double2* gram,
                                                           double2* vwork, int max_bond, double cutoff,
-                                                          double2* vsel, double2* tensors, int chi) {
+                                                          double2* vsel, double2* tensors, int chi,
+                                                          float2* scratch32, double fine) {
   __shared__ JacobiShared<double2, double> js64;
   __shared__ JacobiShared<float2, float> js32;
   __shared__ double s_floor;
@@ -333,7 +337,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   const int ld = in_smem ? w + 1 : w;   // padded rows: column walks hit distinct banks
   double2* G = in_smem ? eig_sm : Gg;
   double2* V = in_smem ? eig_sm + w * ld : Vg;
-  double2* Sc = eig_sm + 2 * w * ld;    // scratch (shared memory path only)
+  double2* Sc = in_smem ? eig_sm + 2 * w * ld : vsel + (int64_t)b * WW;   // FP64 scratch
+  float2* G32 = in_smem ? reinterpret_cast<float2*>(Sc) : scratch32 + (int64_t)b * 2 * TT_SPLIT * WW;
+  float2* V32 = G32 + w * ld;
   if (in_smem)
     for (int e = threadIdx.x; e < w * w; e += blockDim.x) G[(e / w) * ld + e % w] = Gg[e];
   __syncthreads();
@@ -348,9 +354,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
   }
   __syncthreads();
   const double tr = s_floor;
-  if (in_smem) {
-    float2* G32 = reinterpret_cast<float2*>(Sc);
-    float2* V32 = G32 + w * ld;
+  {
     for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
       const int i = e / w, j = e % w;
       const double2 g = G[i * ld + j];
@@ -365,7 +369,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     }
     __syncthreads();
     // Newton-Schulz: Sc = (3I - V^H V) / 2, then V <- V Sc row by row (a
-    // warp per row, each lane two columns, written after the warp's reads)
+    // warp per row, each lane up to four columns, written after the warp's reads)
     smem_matmul(V, V, Sc, w, ld, true);
     __syncthreads();
     for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
@@ -377,15 +381,19 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     {
       const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
       for (int row = warp; row < w; row += nwarps) {
-        double2 o0 = czero(), o1 = czero();
+        double2 o[TT_MAXW / 32];
+#pragma unroll
+        for (int q = 0; q < TT_MAXW / 32; ++q) o[q] = czero();
         for (int k = 0; k < w; ++k) {
           const double2 v = V[row * ld + k];
-          if (lane < w) o0 = cadd(o0, cmul(v, Sc[k * ld + lane]));
-          if (lane + 32 < w) o1 = cadd(o1, cmul(v, Sc[k * ld + lane + 32]));
+#pragma unroll
+          for (int q = 0; q < TT_MAXW / 32; ++q)
+            if (lane + 32 * q < w) o[q] = cadd(o[q], cmul(v, Sc[k * ld + lane + 32 * q]));
         }
         __syncwarp();
-        if (lane < w) V[row * ld + lane] = o0;
-        if (lane + 32 < w) V[row * ld + lane + 32] = o1;
+#pragma unroll
+        for (int q = 0; q < TT_MAXW / 32; ++q)
+          if (lane + 32 * q < w) V[row * ld + lane + 32 * q] = o[q];
       }
     }
     __syncthreads();
@@ -395,15 +403,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     smem_matmul(V, Sc, G, w, ld, true);
     __syncthreads();
     for (int i = threadIdx.x; i < w; i += blockDim.x) G[i * ld + i].y = 0.0;
-  } else {
-    for (int e = threadIdx.x; e < w * w; e += blockDim.x) V[(e / w) * ld + e % w] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
   // After the FP32 stage the FP64 sweeps stop at 1e-13 of the trace (three
   // orders below the 1e-10 cutoff; eigenvalues move by about 1e-15 of the
   // trace against 1e-15): the remaining rotations are the null-space
   // cluster's rounding noise.
-  jacobi_run<double2, double>(G, V, w, ld, 1e-15, (in_smem ? 1e-13 : 1e-15) * tr, 40, js64);
+  jacobi_run<double2, double>(G, V, w, ld, 1e-15, fine * tr, 40, js64);
   if (threadIdx.x == 0) {
     for (int i = 0; i < w; ++i) { s_perm[i] = i; s_lam[i] = G[i * ld + i].x; }
     for (int i = 1; i < w; ++i) {
@@ -555,7 +561,8 @@ void launch_tt_gram(const BatchDev& bd, int step, const float2* sv, const float2
 }
 
 void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, double2* vwork, int max_bond,
-                   double cutoff, double2* vsel, double2* tensors, int chi, cudaStream_t s) {
+                   double cutoff, double2* vsel, double2* tensors, int chi, double2* scratch, double fine,
+                   cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_tt_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_EIG_SMEM);
@@ -563,7 +570,7 @@ void launch_tt_eig(const BatchDev& bd, int step, int* bonds, double2* gram, doub
   }
   qm_note_launch();
   k_tt_eig<<<bd.B, BLOCK_THREADS, TT_EIG_SMEM, s>>>(bd, step, bonds, gram, vwork, max_bond, cutoff, vsel, tensors,
-                                                    chi);
+                                                    chi, reinterpret_cast<float2*>(scratch), fine);
 }
 
 void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const float2* src, float2* dst,

@@ -116,6 +116,19 @@ class Plan:
         """An uninitialised statevector-sized device buffer of this plan."""
         return torch.empty(self.vec_elems * 2, dtype=self.vdtype, device="cuda")
 
+    def buf(self, name: str, numel: int, dtype, zero: bool = False) -> torch.Tensor:
+        """A device buffer kept on the plan under `name` (reallocated only
+        when its size or type changes), so that repeated calls present the
+        same addresses to the library and its stage graphs replay."""
+        store = self.__dict__.setdefault("_bufs", {})
+        t = store.get(name)
+        if t is None or t.numel() != numel or t.dtype != dtype:
+            t = torch.empty(numel, dtype=dtype, device="cuda")
+            store[name] = t
+        if zero:
+            t.zero_()
+        return t
+
     def chi_eff(self, b: int) -> int:
         return min(self.max_bond, 2 ** (self.nqubits[b] // 2))
 
@@ -216,21 +229,27 @@ class Engine:
         return ns, np.concatenate(parts)
 
     # ---- stages --------------------------------------------------------------
-    def upload(self, statevectors, max_layers: int, max_bond: int, precision: str = "fast"):
+    def upload(self, statevectors, max_layers: int, max_bond: int, precision: str = "fast", reuse: bool = False):
         """Plan the batch and copy the (Ket-normalised) statevectors to the device."""
         ns, host = self.pack(statevectors, np.complex128 if precision == "exact" else np.complex64)
         p = self.plan(ns, max_layers, max_bond, precision)
         pinned = torch.from_numpy(host.view(np.float64 if precision == "exact" else np.float32)).pin_memory()
-        sv = p.vec()
+        sv = p.buf("input", p.vec_elems * 2, p.vdtype) if reuse else p.vec()
         sv.copy_(pinned, non_blocking=True)
         return p, sv
 
-    def stage_mps(self, p: Plan, sv: torch.Tensor, bond_dimension: int, stream=None):
-        """(a) statevector -> MPS: site tensors, bonds and the dense truncated target."""
+    def stage_mps(self, p: Plan, sv: torch.Tensor, bond_dimension: int, stream=None, reuse: bool = False):
+        """(a) statevector -> MPS: site tensors, bonds and the dense truncated target.
+        ``reuse``: write into the plan's own stage buffers (``Plan.buf``)."""
         sp = self._sp(stream)
-        tensors = torch.empty(max(p.tensor_elems, 1) * 2, dtype=torch.float64, device="cuda")
-        bonds = torch.empty(p.B * (p.max_n + 1), dtype=torch.int32, device="cuda")
-        target = p.vec()
+        if reuse:
+            tensors = p.buf("tensors", max(p.tensor_elems, 1) * 2, torch.float64)
+            bonds = p.buf("bonds", p.B * (p.max_n + 1), torch.int32)
+            target = p.buf("target", p.vec_elems * 2, p.vdtype)
+        else:
+            tensors = torch.empty(max(p.tensor_elems, 1) * 2, dtype=torch.float64, device="cuda")
+            bonds = torch.empty(p.B * (p.max_n + 1), dtype=torch.int32, device="cuda")
+            target = p.vec()
         self.hd.check(self.lib.qmprs_mps_from_statevector(p.p, _ptr(sv), int(bond_dimension), 1e-10,
                                                           _ptr(tensors), _ptr(bonds), _ptr(target), sp))
         return tensors, bonds, target
@@ -242,38 +261,50 @@ class Engine:
         return out
 
     def stage_layers(self, p: Plan, target: torch.Tensor, num_layers: int, fidelity_threshold: float,
-                     stream=None):
+                     stream=None, reuse: bool = False):
         """(b)+(c) disentangling layers from the dense target."""
         sp = self._sp(stream)
-        gates = torch.zeros(p.gate_elems * 2, dtype=torch.float64, device="cuda")
-        arity = torch.zeros(p.gate_elems // 16, dtype=torch.int8, device="cuda")
-        nl = torch.zeros(p.B, dtype=torch.int32, device="cuda")
-        lf = torch.zeros(p.B * num_layers * 2, dtype=torch.float64, device="cuda")
+        if reuse:
+            gates = p.buf("gates", p.gate_elems * 2, torch.float64, zero=True)
+            arity = p.buf("arity", p.gate_elems // 16, torch.int8, zero=True)
+            nl = p.buf("nl", p.B, torch.int32, zero=True)
+            lf = p.buf("lf", p.B * num_layers * 2, torch.float64, zero=True)
+        else:
+            gates = torch.zeros(p.gate_elems * 2, dtype=torch.float64, device="cuda")
+            arity = torch.zeros(p.gate_elems // 16, dtype=torch.int8, device="cuda")
+            nl = torch.zeros(p.B, dtype=torch.int32, device="cuda")
+            lf = torch.zeros(p.B * num_layers * 2, dtype=torch.float64, device="cuda")
         self.hd.check(self.lib.qmprs_unitary_layers(p.p, _ptr(target), int(num_layers), float(fidelity_threshold),
                                                     _ptr(gates), _ptr(arity), _ptr(nl), _ptr(lf), sp))
         return gates, arity, nl, lf
 
     def stage_sweeps(self, p: Plan, target, gates, arity, nl, num_sweeps: int, stop_fidelity: float = 0.0,
-                     stream=None):
-        """(d) environment sweeps; returns per-sweep fidelities and sweeps run."""
+                     stream=None, reuse: str = ""):
+        """(d) environment sweeps; returns per-sweep fidelities and sweeps run.
+        ``reuse``: a name under which the plan keeps the output buffers."""
         sp = self._sp(stream)
         S = max(int(num_sweeps), 0)
-        sf = torch.zeros(max(p.B * S, 1), dtype=torch.float64, device="cuda")
-        sd = torch.zeros(p.B, dtype=torch.int32, device="cuda")
+        if reuse:
+            sf = p.buf(reuse + "_sf", max(p.B * S, 1), torch.float64, zero=True)
+            sd = p.buf(reuse + "_sd", p.B, torch.int32, zero=True)
+        else:
+            sf = torch.zeros(max(p.B * S, 1), dtype=torch.float64, device="cuda")
+            sd = torch.zeros(p.B, dtype=torch.int32, device="cuda")
         if S > 0:
             self.hd.check(self.lib.qmprs_optimize_layers(p.p, _ptr(target), _ptr(gates), _ptr(arity), _ptr(nl), S,
                                                          float(stop_fidelity), _ptr(sf), _ptr(sd), sp))
         return sf, sd
 
-    def stage_circuit(self, p: Plan, gates, arity, nl, stream=None) -> torch.Tensor:
+    def stage_circuit(self, p: Plan, gates, arity, nl, stream=None, reuse: str = "") -> torch.Tensor:
         sp = self._sp(stream)
-        circ = p.vec()
+        circ = p.buf(reuse + "_circ", p.vec_elems * 2, p.vdtype) if reuse else p.vec()
         self.hd.check(self.lib.qmprs_circuit_state(p.p, _ptr(gates), _ptr(arity), _ptr(nl), _ptr(circ), sp))
         return circ
 
-    def overlap(self, p: Plan, a: torch.Tensor, b: torch.Tensor, stream=None) -> torch.Tensor:
+    def overlap(self, p: Plan, a: torch.Tensor, b: torch.Tensor, stream=None, reuse: str = "") -> torch.Tensor:
         sp = self._sp(stream)
-        ov = torch.zeros(p.B * 2, dtype=torch.float64, device="cuda")
+        ov = p.buf(reuse + "_ov", p.B * 2, torch.float64) if reuse else torch.zeros(p.B * 2, dtype=torch.float64,
+                                                                                       device="cuda")
         self.hd.check(self.lib.qmprs_overlap(p.p, _ptr(a), _ptr(b), _ptr(ov), sp))
         return ov
 
@@ -426,8 +457,8 @@ class Engine:
         fid = torch.sqrt(ov[0::2] ** 2 + ov[1::2] ** 2) / torch.sqrt(nn[0::2])
         if not bool((fid < stop_fidelity).any().item()):
             return gates, sf, sd, ov
-        sf2, sd2 = self.stage_sweeps(p, target, analytic, arity, nl, num_sweeps, stop_fidelity)
-        ov2 = self.overlap(p, self.stage_circuit(p, analytic, arity, nl), sv)
+        sf2, sd2 = self.stage_sweeps(p, target, analytic, arity, nl, num_sweeps, stop_fidelity, reuse="fb")
+        ov2 = self.overlap(p, self.stage_circuit(p, analytic, arity, nl, reuse="fb"), sv, reuse="fb")
         fid2 = torch.sqrt(ov2[0::2] ** 2 + ov2[1::2] ** 2) / torch.sqrt(nn[0::2])
         take = (fid < stop_fidelity) & (fid2 > fid)                       # per state
         per_slot = torch.repeat_interleave(take, torch.as_tensor(
@@ -490,13 +521,18 @@ class Engine:
         from its analytic layers (the plain method) and keeps the better of
         the two results.
 
+        The stage outputs live in buffers kept on the plan (``Plan.buf``),
+        so that repeated calls replay the library's stage graphs; with
+        ``download=False`` the returned device tensors are those buffers and
+        stay valid until the next ``encode`` on the same plan.
+
         ``precision="exact"`` runs the double-float mode
         (``QMPRS_PRECISION_EXACT``): a packed buffer is then float64 pairs
         (complex128), and the per-layer and per-sweep fidelities follow an
         FP64 run of the reference's algorithm.
         """
         if nqubits is None:
-            p, sv = self.upload(statevectors, num_layers, bond_dimension, precision)
+            p, sv = self.upload(statevectors, num_layers, bond_dimension, precision, reuse=True)
         else:
             p = self.plan(nqubits, num_layers, bond_dimension, precision)
             sv = statevectors
@@ -504,17 +540,18 @@ class Engine:
                 raise ValueError("packed statevector buffer does not match the qubit counts and precision")
             if not sv.is_cuda:
                 sv = self._stage_input(p, sv)
-        tensors, bonds, target = self.stage_mps(p, sv, bond_dimension)
-        gates, arity, nl, lf = self.stage_layers(p, target, num_layers, fidelity_threshold)
+        tensors, bonds, target = self.stage_mps(p, sv, bond_dimension, reuse=True)
+        gates, arity, nl, lf = self.stage_layers(p, target, num_layers, fidelity_threshold, reuse=True)
         analytic = None
         if warm_start is not None:
             from . import warmstart as _ws
-            analytic = gates.clone()
+            analytic = p.buf("analytic", gates.numel(), gates.dtype)
+            analytic.copy_(gates)
             _ws.predict_layers(warm_start, gates, p.gate_off, p.nqubits, nl.cpu().numpy())
-        sf, sd = self.stage_sweeps(p, target, gates, arity, nl, num_sweeps, stop_fidelity)
-        circ = self.stage_circuit(p, gates, arity, nl)
-        ov = self.overlap(p, circ, sv)
-        nn = self.overlap(p, sv, sv)
+        sf, sd = self.stage_sweeps(p, target, gates, arity, nl, num_sweeps, stop_fidelity, reuse="main")
+        circ = self.stage_circuit(p, gates, arity, nl, reuse="main")
+        ov = self.overlap(p, circ, sv, reuse="ov")
+        nn = self.overlap(p, sv, sv, reuse="nn")
         if analytic is not None and stop_fidelity > 0.0:
             gates, sf, sd, ov = self._fallback(p, target, sv, analytic, gates, arity, nl, sf, sd, ov, nn,
                                                num_sweeps, stop_fidelity)

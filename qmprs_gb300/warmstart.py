@@ -220,7 +220,9 @@ class WarmStartMLP:
             dZb=torch.zeros(B, max(hid), dtype=bf, device=d),
             dZT=torch.zeros(max(hid), B, dtype=bf, device=d),
             loss=torch.zeros(B, dtype=f, device=d),
-            part=torch.zeros(max(1, B // 512) * max(DIMS) * max(DIMS), dtype=f, device=d),
+            # split-K partials: ceil(K / 512) blocks of M x N for K = B (the
+            # backward GEMMs), as qmprs_gemm_bf16 requires
+            part=torch.zeros(max(1, -(-B // 512)) * max(DIMS) * max(DIMS), dtype=f, device=d),
         )
         self._bufs[B] = buf
         return buf

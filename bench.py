@@ -25,7 +25,8 @@ sweeps -> circuit state -> fidelity) over the batch.
   (32 B per amplitude of every state the pass touches: read and write psi
   and t; 16 B for a state's first group, which only reads) over its
   event-timed launches in a profiled pass of the same batch, against the
-  measured HBM copy bandwidth.
+  measured HBM copy bandwidth; ``roofline.k_rebuild_pass`` gives the same
+  for the circuit rebuild pass (16 B per amplitude).
 * ``cpu_baseline``  the FP64 oracle's call-by-call restatement of the
   reference (``oracle.mpsops``, literal conventions, one state per process,
   OPENBLAS_NUM_THREADS=1, sweeps stopping at 0.98) on states of the batch
@@ -429,6 +430,8 @@ def run_gpu(args, rank, world):
     peak, peak_kind = peaks()
     n_env, ms_env, by_env = prof[0]
     achieved = (by_env / n_env) / (ms_env / n_env * 1e-3) / 1e9 if n_env and ms_env > 0 else 0.0
+    n_rb, ms_rb, by_rb = prof[2]
+    achieved_rb = by_rb / (ms_rb * 1e-3) / 1e9 if n_rb and ms_rb > 0 else 0.0
 
     # ---- max over ranks
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], world, "cuda")
@@ -471,7 +474,12 @@ def run_gpu(args, rank, world):
                      "launches": n_env, "avg_launch_us": ms_env / max(n_env, 1) * 1e3,
                      "bytes_per_launch": by_env / max(n_env, 1),
                      "sweep_kernel_ms": {"group_pass": prof[0][1], "group_polar": prof[3][1],
-                                         "rebuild": prof[2][1]}},
+                                         "rebuild": prof[2][1]},
+                     "k_rebuild_pass": {"achieved": achieved_rb, "frac": achieved_rb / peak, "launches": n_rb,
+                                        "avg_launch_us": ms_rb / max(n_rb, 1) * 1e3,
+                                        "bytes_per_launch": by_rb / max(n_rb, 1),
+                                        "note": "16 B per amplitude (read and write C|0>) of every state the "
+                                                "launch touches"}},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{len(cpu_samples)} states of the benchmark batch (qubits 12-17, replayed from "
                                    "its seed), one per core, oracle restatement of the reference (literal "

@@ -135,6 +135,17 @@ int qmprs_plan_set_graphs(qmprs_plan_t p, int enable);
 int qmprs_plan_graph_stats(qmprs_plan_t p, int* cached, int64_t* replays);
 
 /*
+ * Counters of the eigensolver for Grams wider than 128 (bonds above 64) in
+ * qmprs_mps_from_statevector, summed over the plan's calls: Grams solved,
+ * FP32 block-Jacobi sweeps, FP64 refinement steps, and the largest
+ * first-order correction of the last step of any Gram (the error left is
+ * about its square).
+ * Replaces: nothing (a diagnostic of the SVD that quimb's compression runs
+ * in qmprs/primitives/mps.py:242,247).
+ */
+int qmprs_plan_wide_stats(qmprs_plan_t p, int* grams, int* sweeps, int* refine_steps, float* last_correction);
+
+/*
  * Autotuner of the sweep's tile passes (on by default).  The grouped sweep
  * and the circuit rebuild run grid-stride loops over chunks of 32 tiles of
  * 2^11 amplitudes; how many blocks take them decides how evenly states of

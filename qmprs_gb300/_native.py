@@ -49,6 +49,8 @@ SIGNATURES: dict[str, tuple] = {
     "qmprs_plan_precision": (ctypes.c_int, [_c_void_p]),
     "qmprs_plan_set_graphs": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
     "qmprs_plan_graph_stats": (ctypes.c_int, [_c_void_p, _c_int_p, _c_i64_p]),
+    "qmprs_plan_wide_stats": (ctypes.c_int, [_c_void_p, _c_int_p, _c_int_p, _c_int_p,
+                                             ctypes.POINTER(ctypes.c_float)]),
     "qmprs_plan_set_autotune": (ctypes.c_int, [_c_void_p, ctypes.c_int]),
     "qmprs_plan_tuning": (ctypes.c_int, [_c_void_p, _c_int_p, _c_int_p]),
     "qmprs_plan_upload": (ctypes.c_int, [_c_void_p, _c_void_p, ctypes.c_int64, _c_void_p, ctypes.POINTER(_c_void_p)]),

@@ -51,11 +51,10 @@ struct qmprs_plan {
   int *d_chunk_state = nullptr, *d_chunk_idx = nullptr, *d_state_chunk0 = nullptr, *d_state_nchunks = nullptr,
       *d_ngroups = nullptr, *d_nrgroups = nullptr;
   GroupEnt *d_grp = nullptr, *d_rgrp = nullptr;
-  // stage (a) beyond bond 64: device-wide Jacobi scratch
+  // stage (a) beyond bond 64: blocked eigensolver scratch
   int tt_w = TT_MAXW, tt_b = TT_MAXB;
-  WJRot* d_wj_rot = nullptr;
-  int *d_wj_count = nullptr, *d_wj_perm = nullptr;
-  double *d_wj_trace = nullptr, *d_wj_lam = nullptr;
+  BJScratch bj, bj_sub;   // blocked eigensolver of Grams wider than TT_MAXW, its deflated subproblem
+  BJStats bj_stats;
   double2 *d_old_gates = nullptr, *d_gpartials = nullptr;
   GroupDev gd;
   // profiling of the sweep kernels (kernel classes: 0 environment stream,
@@ -339,13 +338,7 @@ int ensure_tt_scratch(qmprs_plan* p) {
   CK(dalloc(&p->gram, (int64_t)p->B * WW));
   CK(dalloc(&p->vsel2, (int64_t)p->B * WW));
   CK(dalloc(&p->vwork, (int64_t)p->B * WW));
-  if (p->tt_b > TT_MAXB) {
-    CK(cudaMalloc(reinterpret_cast<void**>(&p->d_wj_rot), wj_rot_bytes(p->tt_w)));
-    CK(dalloc(&p->d_wj_count, 1));
-    CK(dalloc(&p->d_wj_trace, 1));
-    CK(dalloc(&p->d_wj_perm, p->tt_w));
-    CK(dalloc(&p->d_wj_lam, p->tt_w));
-  }
+  if (2 * p->tt_b > p->bd.eig_wmax) CK((cudaError_t)bj_alloc(p->bj, p->tt_w, p->tt_b));
   return QMPRS_OK;
 }
 
@@ -430,7 +423,7 @@ int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, d
       if (r < 1 || r > p->tt_b) continue;
       launch_x_gram(src + p->vec_off[b], ipow2(c), 2 * r, p->tt_partials + (int64_t)b * TT_SPLIT * WW, WW,
                     p->gram + (int64_t)b * WW, s);
-      wide = wide || 2 * r > TT_MAXW;
+      wide = wide || 2 * r > p->bd.eig_wmax;
     }
     launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond,
                   p->tt_partials, 1e-15, s);
@@ -439,11 +432,10 @@ int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, d
         const int c = p->n[b] - 1 - j;
         if (c < 1) continue;
         const int r = hb[(size_t)b * stride + c + 1];
-        if (r < 1 || r > p->tt_b || 2 * r <= TT_MAXW) continue;
-        const int e = tt_wide_eig(p->bd, b, c, 2 * r, p->gram, p->vwork, p->d_wj_rot, p->d_wj_count, p->d_wj_trace,
-                                  p->d_wj_perm, p->d_wj_lam, bonds, p->vsel2, tensors, p->max_bond, max_bond, cutoff,
-                                  s);
-        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) device-wide Jacobi");
+        if (r < 1 || r > p->tt_b || 2 * r <= p->bd.eig_wmax) continue;
+        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, p->bj, p->bj_sub, bonds, p->vsel2, tensors, p->max_bond,
+                                   max_bond, cutoff, BJ_TOL_EXACT, s, &p->bj_stats);
+        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) blocked eigensolver");
       }
     }
     if ((rc = read_ints(p, bonds, hb, s)) != QMPRS_OK) return rc;
@@ -635,10 +627,11 @@ void qmprs_plan_destroy(qmprs_plan_t p) {
                   p->bonds,    p->active,       p->nlayers,    p->num_active,    p->nuc,
                   p->sq,       p->tnorm,        p->d_chunk_state, p->d_chunk_idx, p->d_state_chunk0,
                   p->d_state_nchunks, p->d_ngroups, p->d_grp,    p->d_old_gates,   p->d_gpartials,
-                  p->d_rgrp,   p->d_nrgroups,   p->d_wj_rot,  p->d_wj_count,  p->d_wj_perm,
-                  p->d_wj_trace, p->d_wj_lam, p->d_input, p->X0, p->X1, p->X2, p->XT};
+                  p->d_rgrp,   p->d_nrgroups,   p->d_input, p->X0, p->X1, p->X2, p->XT};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  bj_free(p->bj);
+  bj_free(p->bj_sub);
   delete p;
 }
 
@@ -803,6 +796,7 @@ int qmprs_plan_create(qmprs_handle_t h, int num_states, const int* num_qubits, i
   bd.err = p->d_err;
   bd.tt_w = p->tt_w;
   bd.tt_b = p->tt_b;
+  bd.eig_wmax = num_states <= BJ_SMALL_BATCH ? TT_MAXB : TT_MAXW;
   *out = p;
   return QMPRS_OK;
 }
@@ -862,6 +856,15 @@ int qmprs_plan_graph_stats(qmprs_plan_t p, int* cached, int64_t* replays) {
   return QMPRS_OK;
 }
 
+int qmprs_plan_wide_stats(qmprs_plan_t p, int* grams, int* sweeps, int* refine_steps, float* last_correction) {
+  if (!p) return QMPRS_ERR_INVALID;
+  if (grams) *grams = p->bj_stats.calls;
+  if (sweeps) *sweeps = p->bj_stats.sweeps;
+  if (refine_steps) *refine_steps = p->bj_stats.refine_steps;
+  if (last_correction) *last_correction = p->bj_stats.last_emax;
+  return QMPRS_OK;
+}
+
 int qmprs_plan_upload(qmprs_plan_t p, const void* host, int64_t bytes, void* stream, void** dev_out) {
   if (!p || !host || !dev_out) return QMPRS_ERR_INVALID;
   *dev_out = nullptr;
@@ -899,7 +902,9 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
   if (p->precision == QMPRS_PRECISION_EXACT)
     return exact_mps_from_statevector(p, (const double2*)sv_, max_bond, cutoff, tensors, bonds, (double2*)target_, s);
   const int64_t WW = (int64_t)p->tt_w * p->tt_w;
-  const bool wide = p->tt_b > TT_MAXB;
+  const bool wide = 2 * p->tt_b > p->bd.eig_wmax;
+  // the first step at which a Gram can be wider than eig_wmax (bond 2^(j+1))
+  const int jwide = p->bd.eig_wmax >= TT_MAXW ? 6 : 5;
   {
     const int rc = ensure_tt_scratch(p);
     if (rc != QMPRS_OK) return rc;
@@ -923,9 +928,10 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
     launch_tt_eig(p->bd, j, bonds, p->gram, p->vwork, max_bond, cutoff, p->vsel2, tensors, p->max_bond,
                   p->tt_partials, 1e-13, s);
     launch_tt_project(p->bd, j, sv, src, buf[j & 1], bonds, p->vsel2, s);
-    // Grams wider than 128 and projections to more than 64 columns: the
-    // device-wide path, state by state (possible only after 6 cuts)
-    if (wide && j >= 6) {
+    // Grams wider than eig_wmax and projections to more than 64 columns:
+    // the blocked eigensolver and tiled products, state by state (possible
+    // only from step jwide on)
+    if (wide && j >= jwide) {
       int rc = read_bonds();
       if (rc != QMPRS_OK) return rc;
       bool any = false;
@@ -933,11 +939,10 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
         const int c = p->n[b] - 1 - j;
         if (c < 1) continue;
         const int r = hb[(size_t)b * stride + c + 1];
-        if (r < 1 || r > p->tt_b || 2 * r <= TT_MAXW) continue;
-        const int e = tt_wide_eig(p->bd, b, c, 2 * r, p->gram, p->vwork, p->d_wj_rot, p->d_wj_count,
-                                  p->d_wj_trace, p->d_wj_perm, p->d_wj_lam, bonds, p->vsel2, tensors,
-                                  p->max_bond, max_bond, cutoff, s);
-        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) device-wide Jacobi");
+        if (r < 1 || r > p->tt_b || 2 * r <= p->bd.eig_wmax) continue;
+        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, p->bj, p->bj_sub, bonds, p->vsel2, tensors, p->max_bond,
+                                   max_bond, cutoff, BJ_TOL_FAST, s, &p->bj_stats);
+        if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) blocked eigensolver");
         any = true;
       }
       if (any) {
@@ -949,7 +954,7 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
         if (c < 1) continue;
         const int r = hb[(size_t)b * stride + c + 1], keep = hb[(size_t)b * stride + c];
         if (r < 1 || keep < 1 || r > p->tt_b || keep > p->tt_b) continue;
-        if (2 * r <= TT_MAXW && keep <= TT_MAXB) continue;
+        if (2 * r <= p->bd.eig_wmax && keep <= TT_MAXB) continue;
         const int w = 2 * r;
         const float2* m = src + p->vec_off[b];
         launch_cgemm(m, w, p->vsel2 + (int64_t)b * WW, p->tt_b, buf[j & 1] + p->vec_off[b], keep, ipow2(c), keep, w,

@@ -74,7 +74,12 @@ struct BatchDev {
   int* err;                // [1] error flag bits
   int tt_w;                // stage (a): Gram stride (>= TT_MAXW, 2 x the largest bond)
   int tt_b;                // stage (a): largest bond / selected-column stride (>= TT_MAXB)
+  int eig_wmax;            // stage (a): widest Gram of the one-block eigensolver; wider ones
+                           // take the blocked solver (ttsvd_wide.cu)
 };
+// Batches of at most this many states send Grams wider than 64 to the
+// blocked multi-SM solver: one block per state would leave the GPU idle
+#define BJ_SMALL_BATCH 8
 
 // Gate selection modes for the per-step gate launches.
 enum {
@@ -188,13 +193,38 @@ void launch_tt_project(const BatchDev& bd, int step, const float2* sv, const flo
                        const int* bonds, const double2* vsel, cudaStream_t s);
 void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1, const int* bonds,
                      double2* tensors, int chi, const double2* in_sq, cudaStream_t s);
-struct WJRot;
-int tt_wide_eig(const BatchDev& bd, int b, int c, int w, double2* gram, double2* vwork, WJRot* rot, int* d_count,
-                double* d_trace, int* perm, double* lam, int* bonds, double2* vsel, double2* tensors, int chi,
-                int max_bond, double cutoff, cudaStream_t s);
+// Scratch of the blocked eigensolver for Grams wider than TT_MAXW (one
+// state at a time): FP32 matrix and eigenvectors (W x W, W = width rounded
+// up to 32), the subproblem rotations, the FP64 basis X, the input of a
+// deflated subproblem H, two FP64 work matrices, and the refinement
+// products [H X_K | X_K] and [S | X^H X_K] (n x 2K).
+struct BJScratch {
+  int W = 0, kmax = 0;
+  float2 *A = nullptr, *V = nullptr, *J = nullptr;
+  double2 *X = nullptr, *H = nullptr, *T = nullptr, *T2 = nullptr, *YX = nullptr, *SR = nullptr;
+  int *perm = nullptr, *order = nullptr, *count = nullptr;
+  double *lamA = nullptr, *lamK = nullptr, *lsort = nullptr, *stats = nullptr, *part = nullptr;
+  unsigned* emax = nullptr;
+};
+// refinement tolerance on max |E| (the error after a step is about its
+// square): exact mode to FP64 level, fast mode to about 1e-8
+#define BJ_TOL_EXACT 1e-7
+#define BJ_TOL_FAST 1e-4
+// eigenvalues above this fraction of the largest count as resolved by the
+// FP32 sweeps; the rest form the deflated subproblem when it holds columns
+// that may be kept
+#define BJ_RESOLVED 1e-5
+struct BJStats {
+  int calls = 0, sweeps = 0, refine_steps = 0;
+  float last_emax = 0.f;
+};
+int bj_alloc(BJScratch& sc, int tt_w, int tt_b);
+void bj_free(BJScratch& sc);
+int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, BJScratch& sc, BJScratch& sub,
+                 int* bonds, double2* vsel, double2* tensors, int chi, int max_bond, double cutoff, double refine_tol,
+                 cudaStream_t s, BJStats* st);
 void launch_cgemm(const float2* A, int64_t lda, const double2* B, int64_t ldb, float2* C, int64_t ldc, int64_t M,
                   int N, int K, cudaStream_t s);
-size_t wj_rot_bytes(int w);
 void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,
                          const float2* src, float2* dst_buf, float2* target, cudaStream_t s);
 

@@ -16,8 +16,10 @@
 // as quimb's rsum2 renormalisation does) and k_mps_contract rebuilds the
 // truncated dense target, left to right.
 //
-// Supported widths: w <= TT_MAXW (bonds <= TT_MAXB).  A state whose Gram
-// would be wider raises KERR_EIG_WIDTH and has its bond poisoned (-1); every
+// Widths: the one-block kernels take Grams up to bd.eig_wmax (128, or 64 in
+// batches of at most BJ_SMALL_BATCH states); wider ones are diagonalised by
+// the blocked solver (ttsvd_wide.cu).  A state whose bond exceeds the plan's
+// capacity raises KERR_EIG_WIDTH and has its bond poisoned (-1); every
 // later kernel of the stage skips a state whose bonds are out of range, so
 // no access ever depends on an unset bond.
 #include "device_common.cuh"
@@ -329,7 +331,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_eig(BatchDev bd, int step,
     return;
   }
   const int w = 2 * r;
-  if (w > TT_MAXW) return;   // diagonalised by the device-wide solver (ttsvd_wide.cu)
+  if (w > bd.eig_wmax) return;   // diagonalised by the blocked solver (ttsvd_wide.cu)
   extern __shared__ double2 eig_sm[];
   double2* Gg = gram + (int64_t)b * WW;
   double2* Vg = vwork + (int64_t)b * WW;
@@ -461,7 +463,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_project(BatchDev bd, int s
     const int keep = bond[c];
     if (!bond_ok(r, bd.tt_b) || !bond_ok(keep, bd.tt_b)) continue;
     const int w = 2 * r;
-    if (w > TT_MAXW || keep > TT_MAXB) continue;   // projected by k_cgemm
+    if (w > bd.eig_wmax || keep > TT_MAXB) continue;   // projected by k_cgemm
     __syncthreads();
     for (int e = threadIdx.x; e < w * keep; e += blockDim.x) {
       const double2 v = vsel[(int64_t)b * WW + (int64_t)(e / keep) * bd.tt_b + (e % keep)];

@@ -2,163 +2,666 @@
 // same right-to-left truncated SVD as ttsvd.cu, for the configurations with
 // bond dimension 256 (20 qubits) and 1024 (24 qubits).
 //
-// The w x w Gram (w up to 2048) no longer fits one block, so the parallel
-// cyclic Jacobi runs over the whole GPU with one launch per phase of each
-// round (host-driven rounds, no device-wide barrier):
-//   k_wj_params   rotation of every pair of the round (w/2 threads) and a
-//                 rotation count per sweep;
-//   k_wj_cols     G <- G J and V <- V J on the two columns of every pair;
-//   k_wj_rows     G <- J^H G on the two rows of every pair, zeroing the
-//                 eliminated entries.
-// The host reads the rotation count once per sweep and stops when a sweep
-// rotates nothing (at most TTW_MAX_SWEEPS sweeps).  The thresholds are the
-// ones of the one-block solver: relative 1e-15 and an absolute floor of
-// 1e-15 of the trace.
-//   k_wide_finalize  eigenvalue ranks (parallel), quimb's rsum2 cutoff with
-//                 max_bond, canonical phases of the kept eigenvectors, the
-//                 selected columns and the site tensor;
+// The w x w Hermitian Gram (w up to 2048) is diagonalised in two precisions:
+//
+// 1. Blocked two-sided Jacobi in FP32.  The padded width W (a multiple of
+//    32) is cut into blocks of 16 indices; a round pairs the blocks
+//    (round-robin tournament) and every pair is one 32 x 32 subproblem.
+//      k_bj_solve   one block per pair: the subproblem in shared memory,
+//                   one cyclic Jacobi sweep (31 rounds of 16 disjoint
+//                   rotations, each applied to 2 x 2 entry groups), the
+//                   accumulated 32 x 32 unitary J, and the rotated
+//                   diagonal tile written back;
+//      k_bj_update  A[P,Q] <- J_P^H A[P,Q] J_Q on every off-diagonal tile of
+//                   the round (upper triangle, mirrored) and V[:,Q] <- V J_Q.
+//    Sweeps run until one sweep makes no rotation larger than 1e-5 of
+//    sqrt(a_pp a_qq) (at most BJ_MAX_SWEEPS); rotations below FP32
+//    resolution (1e-7 relative, or 1e-7 of ||G||_F absolute) are skipped.
+// 2. FP64 refinement of the K columns that can be kept (K = min(w,
+//    max_bond, bond capacity, 2^c)), and of the discarded ones whose FP32
+//    eigenvalue lies within 1e-5 (of the largest) of the last kept one
+//    (their order and mixing with it are below FP32 resolution), by the
+//    iterative refinement of
+//    Ogita & Aishima (Japan J. Indust. Appl. Math. 35, 2018): with X the
+//    FP32 eigenvectors ordered by eigenvalue,
+//      S = X^H G X_K,  R = I - X^H X_K,  l_j = S_jj / (1 - R_jj),
+//      E_ij = s_ij e_ij,  E_jj = R_jj / 2 + sum_i (c_ij - 1),
+//    where (c_ij, s_ij e_ij) is the rotation that diagonalises the 2 x 2
+//    block [[l_j, conj(b)], [b, l_i]], b = S_ij + l_j R_ij (to first order
+//    E_ij = b / (l_j - l_i), the published step; the full rotation also
+//    resolves near-degenerate pairs), and
+//      X_K <- X_K + X E.
+//    S and R are FP64 products (k_zgemm); the correction X E is small and
+//    taken in FP32 products with an FP64 sum.  A step squares the error, so
+//    one or two steps take FP32 eigenvectors to FP64 accuracy; it repeats
+//    until max |E| is below the mode's tolerance, or stops halving (at most
+//    BJ_MAX_REFINE steps).
+//    FP32 resolves eigenvalues down to about 1e-7 of the largest.  When the
+//    columns that may be kept reach below BJ_RESOLVED of it (rank-deficient
+//    Grams, fast-decaying spectra, where the 1e-10 cutoff decides the
+//    bond), the resolved columns are refined first, the rest of the basis
+//    is projected off them and re-orthonormalised (one FP64 Newton-Schulz
+//    step), and the Gram of that subspace, X_N^H G X_N, whose scale is the
+//    small eigenvalues', is solved by the same two steps.
+// 3. k_bj_finalize: the refined eigenvalues in descending order, quimb's
+//    rsum2 cutoff from the trace (the tail sum is the trace minus the kept
+//    eigenvalues, so the unrefined columns never enter it); k_bj_emit, one
+//    block per kept column: canonical phase, the selected column and the
+//    site tensor of cut c.
+//
 //   k_cgemm       C = A B for a tall complex64 A and a small complex128 B
 //                 (the projection M V of the remainder and the left-to-right
 //                 contraction that rebuilds the dense target): 64 x 64 output
 //                 tiles, K staged in shared memory, 4 x 4 outputs per
 //                 thread.
+//
+// Method references: block Jacobi for the Hermitian eigenproblem (Golub &
+// Van Loan, Matrix Computations, 4th ed., sec. 8.5.5), round-robin
+// ordering (ibid. 8.5.4), the Rutishauser-style stable rotation.
+#include <cstring>
+#include <vector>
+
 #include "device_common.cuh"
 
-#define TTW_THREADS 256
-#define TTW_MAX_SWEEPS 40
+#define BJ_B 16             // block of indices; a pair of blocks is a subproblem
+#define BJ_S 32             // subproblem size
+#define BJ_THREADS 256
+#define BJ_MAX_SWEEPS 24
+#define BJ_MAX_REFINE 4
+#define BJ_PARTS 256        // blocks of the norm reduction (fixed: deterministic sums)
+#define BJ_NOISE 1e-6       // eigenvalues below this fraction of the largest are FP32 noise
+#define BJ_MARGIN 1e-5      // discarded columns this close (of the largest) to the last kept one ...
+#define BJ_EXTRA 32         // ... are refined too, at most this many
 
-struct WJRot {
-  int p, q, flag;
-  double c;
-  double2 se, sce;
-};
-
-__global__ void k_wj_params(const double2* G, int w, int k, double floor_abs, WJRot* rot, int* count) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= w / 2) return;
-  const int t1 = i, t2 = w - 1 - i;
-  int p = t1 == 0 ? 0 : 1 + ((t1 - 1 + k) % (w - 1));
-  int q = 1 + ((t2 - 1 + k) % (w - 1));
-  if (p > q) {
-    const int tmp = p;
-    p = q;
-    q = tmp;
+// Pair i of round k of the round-robin tournament over n (even) indices.
+__host__ __device__ inline void bj_pair(int n, int k, int i, int* p, int* q) {
+  const int t2 = n - 1 - i;
+  int a = i == 0 ? 0 : 1 + ((i - 1 + k) % (n - 1));
+  int b = 1 + ((t2 - 1 + k) % (n - 1));
+  if (a > b) {
+    const int t = a;
+    a = b;
+    b = t;
   }
-  const double2 g = G[(int64_t)p * w + q];
-  const double ag = cabs_(g);
-  const double app = G[(int64_t)p * w + p].x, aqq = G[(int64_t)q * w + q].x;
-  WJRot r;
-  r.p = p;
-  r.q = q;
-  r.flag = !(ag == 0.0 || ag <= 1e-15 * sqrt(fabs(app * aqq)) || ag <= floor_abs);
-  r.c = 1.0;
-  r.se = r.sce = czero();
-  if (r.flag) {
-    const double zeta = (aqq - app) / (2.0 * ag);
-    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-    const double cc = 1.0 / sqrt(1.0 + t * t);
-    const double ss = cc * t;
-    const double2 e = cscale(g, 1.0 / ag);
-    r.c = cc;
-    r.se = cscale(e, ss);
-    r.sce = cscale(cconj(e), ss);
-    atomicAdd(count, 1);
-  }
-  rot[i] = r;
+  *p = a;
+  *q = b;
 }
 
-__global__ void k_wj_cols(double2* G, double2* V, int w, const WJRot* rot) {
-  const int64_t total = (int64_t)(w / 2) * w;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / w), row = (int)(idx % w);
-    const WJRot r = rot[i];
-    if (!r.flag) continue;
-    const int64_t o = (int64_t)row * w;
-    const double2 xp = G[o + r.p], xq = G[o + r.q];
-    G[o + r.p] = csub(cscale(xp, r.c), cmul(r.sce, xq));
-    G[o + r.q] = cadd(cmul(r.se, xp), cscale(xq, r.c));
-    const double2 vp = V[o + r.p], vq = V[o + r.q];
-    V[o + r.p] = csub(cscale(vp, r.c), cmul(r.sce, vq));
-    V[o + r.q] = cadd(cmul(r.se, vp), cscale(vq, r.c));
-  }
+// Global index of local index l (0..31) of pair i in round k: the first 16
+// are block p, the next 16 block q.
+__device__ __forceinline__ int bj_index(int nb, int k, int i, int l) {
+  int p, q;
+  bj_pair(nb, k, i, &p, &q);
+  return (l < BJ_B ? p : q) * BJ_B + (l & (BJ_B - 1));
 }
 
-__global__ void k_wj_rows(double2* G, int w, const WJRot* rot) {
-  const int64_t total = (int64_t)(w / 2) * w;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / w), col = (int)(idx % w);
-    const WJRot r = rot[i];
-    if (!r.flag) continue;
-    const int64_t op = (int64_t)r.p * w, oq = (int64_t)r.q * w;
-    const double2 xp = G[op + col], xq = G[oq + col];
-    double2 np_ = csub(cscale(xp, r.c), cmul(r.se, xq));
-    double2 nq = cadd(cmul(r.sce, xp), cscale(xq, r.c));
-    if (col == r.q) np_ = czero();          // the eliminated pair
-    if (col == r.p) {
-      nq = czero();
-      np_.y = 0.0;                           // real diagonal
+__device__ __forceinline__ float2 fcfma(float2 acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+  return acc;
+}
+__device__ __forceinline__ float2 fcfmac(float2 acc, float2 a, float2 b) {   // acc + conj(a) b
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(-a.y, b.x, acc.y);
+  return acc;
+}
+
+// ---- FP32 blocked Jacobi --------------------------------------------------------------
+
+// A <- G (FP32, padded with zeros to W), V <- I; per-block partial sums of
+// |G_ij|^2 in FP64.
+__global__ void k_bj_load(const double2* G, int w, float2* A, float2* V, int W, double* part) {
+  double acc = 0.0;
+  const int64_t total = (int64_t)W * W;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / W), c = (int)(e % W);
+    float2 a = cf(0.f, 0.f);
+    if (r < w && c < w) {
+      const double2 g = G[(int64_t)r * w + c];
+      acc += cnorm2(g);
+      a = cf((float)g.x, r == c ? 0.f : (float)g.y);
     }
-    if (col == r.q) nq.y = 0.0;
-    G[op + col] = np_;
-    G[oq + col] = nq;
+    A[e] = a;
+    V[e] = cf(r == c ? 1.f : 0.f, 0.f);
+  }
+  double v[1] = {acc};
+  block_sum<1>(v);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// stats[0] = ||G||_F, stats[1] = trace (fixed-order sums).
+__global__ void k_bj_stats(const double* part, int nparts, const double2* G, int w, double* stats) {
+  double v[2] = {0.0, 0.0};
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v[0] += part[i];
+  for (int i = threadIdx.x; i < w; i += blockDim.x) v[1] += G[(int64_t)i * w + i].x;
+  block_sum<2>(v);
+  if (threadIdx.x == 0) {
+    stats[0] = sqrt(v[0]);
+    stats[1] = v[1];
   }
 }
 
-__global__ void k_wj_init(const double2* G, double2* V, int w, double* trace) {
-  const int64_t total = (int64_t)w * w;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
-    V[e] = cd((e / w) == (e % w) ? 1.0 : 0.0, 0.0);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    double tr = 0.0;
-    for (int i = 0; i < w; ++i) tr += fabs(G[(int64_t)i * w + i].x);
-    *trace = tr;
+// One block per pair of round k: one Jacobi sweep of the 32 x 32
+// subproblem; J (32 x 32, row-major) to Jbuf[pair]; the rotated diagonal
+// tile back into A.  count += rotations above 1e-5 relative.
+__global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int nb, int k, float2* Jbuf,
+                                                         const double* stats, int* count) {
+  __shared__ float2 a[BJ_S][BJ_S + 1];
+  __shared__ float2 j[BJ_S][BJ_S + 1];
+  __shared__ float rc[BJ_S / 2];
+  __shared__ float2 rse[BJ_S / 2], rsce[BJ_S / 2];
+  __shared__ int rflag[BJ_S / 2];
+  __shared__ int s_big;
+  const int pair = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) s_big = 0;
+  for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+    const int r = e / BJ_S, c = e % BJ_S;
+    a[r][c] = A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)];
+    j[r][c] = cf(r == c ? 1.f : 0.f, 0.f);
+  }
+  const float floor_abs = 1e-7f * (float)stats[0];
+  __syncthreads();
+  // 2 x 2 entry group of this thread: pairs (gr, gc) of the inner round
+  const int gr = tid / (BJ_S / 2), gc = tid % (BJ_S / 2);
+  for (int ir = 0; ir < BJ_S - 1; ++ir) {
+    if (tid < BJ_S / 2) {
+      int p, q;
+      bj_pair(BJ_S, ir, tid, &p, &q);
+      const float2 g = a[p][q];
+      const float ag = hypotf(g.x, g.y);
+      const float app = a[p][p].x, aqq = a[q][q].x;
+      const float scale = sqrtf(fabsf(app * aqq));
+      const int flag = ag > floor_abs && ag > 1e-7f * scale;
+      rflag[tid] = flag;
+      if (flag) {
+        const float zeta = (aqq - app) / (2.f * ag);
+        const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+        const float c = 1.f / sqrtf(1.f + t * t);
+        const float s = c * t;
+        const float2 e = cf(g.x / ag, g.y / ag);
+        rc[tid] = c;
+        rse[tid] = cf(e.x * s, e.y * s);
+        rsce[tid] = cf(e.x * s, -e.y * s);
+        if (ag > 1e-5f * scale && ag > 1e-6f * (float)stats[0]) s_big = 1;
+      }
+    }
+    __syncthreads();
+    {
+      int pr, qr, pc, qc;
+      bj_pair(BJ_S, ir, gr, &pr, &qr);
+      bj_pair(BJ_S, ir, gc, &pc, &qc);
+      float2 x00 = a[pr][pc], x01 = a[pr][qc], x10 = a[qr][pc], x11 = a[qr][qc];
+      if (rflag[gc]) {   // columns: col_p <- c col_p - s conj(e) col_q ; col_q <- s e col_p + c col_q
+        const float c = rc[gc];
+        const float2 se = rse[gc], sce = rsce[gc];
+        const float2 n00 = cf(c * x00.x - (sce.x * x01.x - sce.y * x01.y), c * x00.y - (sce.x * x01.y + sce.y * x01.x));
+        const float2 n01 = cf(se.x * x00.x - se.y * x00.y + c * x01.x, se.x * x00.y + se.y * x00.x + c * x01.y);
+        const float2 n10 = cf(c * x10.x - (sce.x * x11.x - sce.y * x11.y), c * x10.y - (sce.x * x11.y + sce.y * x11.x));
+        const float2 n11 = cf(se.x * x10.x - se.y * x10.y + c * x11.x, se.x * x10.y + se.y * x10.x + c * x11.y);
+        x00 = n00;
+        x01 = n01;
+        x10 = n10;
+        x11 = n11;
+      }
+      if (rflag[gr]) {   // rows: row_p <- c row_p - s e row_q ; row_q <- s conj(e) row_p + c row_q
+        const float c = rc[gr];
+        const float2 se = rse[gr], sce = rsce[gr];
+        const float2 n00 = cf(c * x00.x - (se.x * x10.x - se.y * x10.y), c * x00.y - (se.x * x10.y + se.y * x10.x));
+        const float2 n01 = cf(c * x01.x - (se.x * x11.x - se.y * x11.y), c * x01.y - (se.x * x11.y + se.y * x11.x));
+        const float2 n10 = cf(sce.x * x00.x - sce.y * x00.y + c * x10.x, sce.x * x00.y + sce.y * x00.x + c * x10.y);
+        const float2 n11 = cf(sce.x * x01.x - sce.y * x01.y + c * x11.x, sce.x * x01.y + sce.y * x01.x + c * x11.y);
+        x00 = n00;
+        x01 = n01;
+        x10 = n10;
+        x11 = n11;
+      }
+      if (gr == gc) {    // the rotated pair: real diagonal, eliminated off-diagonal
+        x00.y = 0.f;
+        x11.y = 0.f;
+        if (rflag[gr]) x01 = x10 = cf(0.f, 0.f);
+      }
+      a[pr][pc] = x00;
+      a[pr][qc] = x01;
+      a[qr][pc] = x10;
+      a[qr][qc] = x11;
+      // J <- J R on the columns of pair (tid % 16), rows tid / 16 and tid / 16 + 16
+      for (int h = 0; h < 2; ++h) {
+        const int row = gr + h * (BJ_S / 2);
+        if (!rflag[gc]) continue;
+        const float c = rc[gc];
+        const float2 se = rse[gc], sce = rsce[gc];
+        const float2 vp = j[row][pc], vq = j[row][qc];
+        j[row][pc] = cf(c * vp.x - (sce.x * vq.x - sce.y * vq.y), c * vp.y - (sce.x * vq.y + sce.y * vq.x));
+        j[row][qc] = cf(se.x * vp.x - se.y * vp.y + c * vq.x, se.x * vp.y + se.y * vp.x + c * vq.y);
+      }
+    }
+    __syncthreads();
+  }
+  float2* jo = Jbuf + (int64_t)pair * BJ_S * BJ_S;
+  for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+    const int r = e / BJ_S, c = e % BJ_S;
+    jo[e] = j[r][c];
+    // Hermitian diagonal tile: the upper triangle and its mirror
+    const float2 v = r <= c ? a[r][c] : cf(a[c][r].x, -a[c][r].y);
+    A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)] = v;
+  }
+  if (tid == 0 && s_big) atomicAdd(count, 1);
+}
+
+// 32 x 32 complex product in shared memory, 4 consecutive outputs per
+// thread (row tid / 8, columns 4 (tid % 8) ...): out = (CONJ ? x^H : x) y.
+template <bool CONJ>
+__device__ __forceinline__ void bj_mm32(const float2 (*x)[BJ_S + 1], const float2 (*y)[BJ_S + 1], float2 (&out)[4]) {
+  const int r = threadIdx.x / 8, c0 = (threadIdx.x % 8) * 4;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) out[i] = cf(0.f, 0.f);
+#pragma unroll 8
+  for (int m = 0; m < BJ_S; ++m) {
+    const float2 xv = CONJ ? x[m][r] : x[r][m];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out[i] = CONJ ? fcfmac(out[i], xv, y[m][c0 + i]) : fcfma(out[i], xv, y[m][c0 + i]);
   }
 }
 
-// Descending order of the diagonal (ties by index), rsum2 cutoff, phases,
-// selected columns (stride vstride) and the site tensor of cut c.  One block.
-__global__ void __launch_bounds__(1024) k_wide_finalize(BatchDev bd, int b, int c, const double2* G, double2* V,
-                                                         int w, int* bonds, double2* vsel, int vstride,
-                                                         double2* tensors, int chi, int max_bond, double cutoff,
-                                                         int* perm, double* lam) {
-  __shared__ int s_keep;
-  for (int i = threadIdx.x; i < w; i += blockDim.x) {
-    const double li = G[(int64_t)i * w + i].x;
+// Blocks [0, nA): off-diagonal tiles P < Q of round k (upper triangle in
+// row order), A[P,Q] <- J_P^H A[P,Q] J_Q and its mirror; blocks [nA, nA +
+// nV): V[R rows, Q] <- V[R rows, Q] J_Q for row tiles R of 32 rows.
+__global__ void __launch_bounds__(BJ_THREADS) k_bj_update(float2* A, float2* V, int W, int nb, int k,
+                                                          const float2* Jbuf, int nA) {
+  __shared__ float2 t[BJ_S][BJ_S + 1];
+  __shared__ float2 jq[BJ_S][BJ_S + 1];
+  __shared__ float2 jp[BJ_S][BJ_S + 1];
+  const int np = nb / 2, tid = threadIdx.x;
+  const int r = tid / 8, c0 = (tid % 8) * 4;
+  float2 out[4];
+  if ((int)blockIdx.x < nA) {
+    // tile index -> (P, Q), P < Q: row P holds np - 1 - P tiles
+    int rem = blockIdx.x, P = 0;
+    while (rem >= np - 1 - P) {
+      rem -= np - 1 - P;
+      ++P;
+    }
+    const int Q = P + 1 + rem;
+    for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+      const int rr = e / BJ_S, cc = e % BJ_S;
+      t[rr][cc] = A[(int64_t)bj_index(nb, k, P, rr) * W + bj_index(nb, k, Q, cc)];
+      jq[rr][cc] = Jbuf[(int64_t)Q * BJ_S * BJ_S + e];
+      jp[rr][cc] = Jbuf[(int64_t)P * BJ_S * BJ_S + e];
+    }
+    __syncthreads();
+    bj_mm32<false>(t, jq, out);   // U = T J_Q
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t[r][c0 + i] = out[i];
+    __syncthreads();
+    bj_mm32<true>(jp, t, out);    // J_P^H U
+    const int gi = bj_index(nb, k, P, r);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int gj = bj_index(nb, k, Q, c0 + i);
+      A[(int64_t)gi * W + gj] = out[i];
+      A[(int64_t)gj * W + gi] = cf(out[i].x, -out[i].y);
+    }
+  } else {
+    const int tI = blockIdx.x - nA;
+    const int R = tI / np, Q = tI % np;
+    for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+      const int rr = e / BJ_S, cc = e % BJ_S;
+      t[rr][cc] = V[(int64_t)(R * BJ_S + rr) * W + bj_index(nb, k, Q, cc)];
+      jq[rr][cc] = Jbuf[(int64_t)Q * BJ_S * BJ_S + e];
+    }
+    __syncthreads();
+    bj_mm32<false>(t, jq, out);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) V[(int64_t)(R * BJ_S + r) * W + bj_index(nb, k, Q, c0 + i)] = out[i];
+  }
+}
+
+// Descending order of the FP32 eigenvalues (diagonal of A, ties by index):
+// perm[rank] = index, lamA[rank] = value.  One block.
+__global__ void __launch_bounds__(1024) k_bj_sort(const float2* A, int W, int n, int* perm, double* lamA) {
+  extern __shared__ float dg[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dg[i] = A[(int64_t)i * W + i].x;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float li = dg[i];
     int rank = 0;
-    for (int j = 0; j < w; ++j) {
-      const double lj = G[(int64_t)j * w + j].x;
+    for (int j = 0; j < n; ++j) {
+      const float lj = dg[j];
       rank += (lj > li) || (lj == li && j < i);
     }
     perm[rank] = i;
-    lam[rank] = li;
+    lamA[rank] = (double)li;
+  }
+}
+
+// X[r][j] = V[r][perm[j]] (r, j < n) in FP64.
+__global__ void k_bj_basis(const float2* V, int W, int n, const int* perm, double2* X) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / n), jc = (int)(e % n);
+    X[e] = f2d(V[(int64_t)r * W + perm[jc]]);
+  }
+}
+
+// ---- FP64 refinement ------------------------------------------------------------------
+
+// C[m][n] = alpha sum_k op(A)[m][k] B[k][n] (+ D[m][n]) in FP64; op(A)[m][k]
+// = A[m][k], or conj(A[k][m]) with CONJ.  64 x 64 tiles, K in chunks of 8,
+// 4 x 4 outputs per thread.
+#define ZG_T 64
+#define ZG_K 8
+template <bool CONJ>
+__global__ void __launch_bounds__(256) k_zgemm(const double2* A, int64_t lda, const double2* B, int64_t ldb,
+                                               const double2* D, int64_t ldd, double2* C, int64_t ldc, int M, int N,
+                                               int K, double alpha) {
+  __shared__ double2 As[ZG_K][ZG_T + 1];
+  __shared__ double2 Bs[ZG_K][ZG_T];
+  const int m0 = blockIdx.x * ZG_T, n0 = blockIdx.y * ZG_T;
+  const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = czero();
+  for (int k0 = 0; k0 < K; k0 += ZG_K) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < ZG_T * ZG_K; e += blockDim.x) {
+      int mm, kk;
+      if (CONJ) {
+        kk = e / ZG_T;
+        mm = e % ZG_T;
+      } else {
+        mm = e / ZG_K;
+        kk = e % ZG_K;
+      }
+      const int gm = m0 + mm, gk = k0 + kk;
+      double2 v = czero();
+      if (gm < M && gk < K) v = CONJ ? cconj(A[(int64_t)gk * lda + gm]) : A[(int64_t)gm * lda + gk];
+      As[kk][mm] = v;
+      const int kb = e / ZG_T, nn = e % ZG_T;
+      const int gkb = k0 + kb, gn = n0 + nn;
+      Bs[kb][nn] = (gkb < K && gn < N) ? B[(int64_t)gkb * ldb + gn] : czero();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZG_K; ++kk) {
+      double2 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][tr * 4 + i];
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) bv[j2] = Bs[kk][tc * 4 + j2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j2 = 0; j2 < 4; ++j2) {
+          acc[i][j2].x = fma(av[i].x, bv[j2].x, acc[i][j2].x);
+          acc[i][j2].x = fma(-av[i].y, bv[j2].y, acc[i][j2].x);
+          acc[i][j2].y = fma(av[i].x, bv[j2].y, acc[i][j2].y);
+          acc[i][j2].y = fma(av[i].y, bv[j2].x, acc[i][j2].y);
+        }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tr * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) {
+      const int gn = n0 + tc * 4 + j2;
+      if (gn >= N) continue;
+      double2 v = cscale(acc[i][j2], alpha);
+      if (D) v = cadd(v, D[(int64_t)gm * ldd + gn]);
+      C[(int64_t)gm * ldc + gn] = v;
+    }
+  }
+}
+
+// C += A B with a small B (the correction X E): FP32 products (exact in FP64
+// after rounding both factors to FP32), FP32 sums over chunks of 8, FP64
+// sums over chunks.  Same tiling as k_zgemm.
+__global__ void __launch_bounds__(256) k_zgemm_small(const double2* A, int64_t lda, const double2* B, int64_t ldb,
+                                                     double2* C, int64_t ldc, int M, int N, int K) {
+  __shared__ float2 As[ZG_K][ZG_T + 1];
+  __shared__ float2 Bs[ZG_K][ZG_T];
+  const int m0 = blockIdx.x * ZG_T, n0 = blockIdx.y * ZG_T;
+  const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = czero();
+  for (int k0 = 0; k0 < K; k0 += ZG_K) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < ZG_T * ZG_K; e += blockDim.x) {
+      const int mm = e / ZG_K, kk = e % ZG_K;
+      const int gm = m0 + mm, gk = k0 + kk;
+      const double2 v = (gm < M && gk < K) ? A[(int64_t)gm * lda + gk] : czero();
+      As[kk][mm] = cf((float)v.x, (float)v.y);
+      const int kb = e / ZG_T, nn = e % ZG_T;
+      const int gkb = k0 + kb, gn = n0 + nn;
+      const double2 u = (gkb < K && gn < N) ? B[(int64_t)gkb * ldb + gn] : czero();
+      Bs[kb][nn] = cf((float)u.x, (float)u.y);
+    }
+    __syncthreads();
+    float2 part[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) part[i][j2] = cf(0.f, 0.f);
+#pragma unroll
+    for (int kk = 0; kk < ZG_K; ++kk) {
+      float2 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][tr * 4 + i];
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) bv[j2] = Bs[kk][tc * 4 + j2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j2 = 0; j2 < 4; ++j2) part[i][j2] = fcfma(part[i][j2], av[i], bv[j2]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = cadd(acc[i][j2], f2d(part[i][j2]));
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tr * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) {
+      const int gn = n0 + tc * 4 + j2;
+      if (gn < N) C[(int64_t)gm * ldc + gn] = cadd(C[(int64_t)gm * ldc + gn], acc[i][j2]);
+    }
+  }
+}
+
+// dst[r][c] = src[r][c] for r < rows, c < cols (row strides lds, ldd).
+__global__ void k_bj_copy(const double2* src, int64_t lds, double2* dst, int64_t ldd, int rows, int cols) {
+  const int64_t total = (int64_t)rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / cols), c = (int)(e % cols);
+    dst[(int64_t)r * ldd + c] = src[(int64_t)r * lds + c];
+  }
+}
+
+// l_j = S_jj / (1 - R_jj) for the Kc refined columns; SR holds [S | X^H X_K]
+// (row stride 2 Kc), so 1 - R_jj is the (j, Kc + j) entry.
+__global__ void k_bj_lam(const double2* SR, int Kc, double* lamK) {
+  const int jc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jc >= Kc) return;
+  const int64_t o = (int64_t)jc * 2 * Kc;
+  lamK[jc] = SR[o + jc].x / SR[o + Kc + jc].x;
+}
+
+// One block per refined column j: E (n x Kc) into the S half of SR.  Every
+// pair (i, j) takes the rotation that diagonalises its 2 x 2 block
+// [[l_j, conj(b)], [b, l_i]], b = S_ij + l_j R_ij: E_ij = s e (e = b / |b|)
+// and cos - 1 into E_jj, next to R_jj / 2.  For a small coupling s e is
+// the first-order b / (l_j - l_i); near-degenerate pairs get the full
+// rotation.  Pairs of eigenvalues both below BJ_NOISE of the largest
+// (lamA[0], below the FP32 sweeps' resolution) and couplings at FP64
+// rounding level take no rotation: between two refined columns they only
+// restore orthonormality (E_ij = R_ij / 2), against an unrefined column
+// nothing (its overlap is that column's own FP32 error).  emax =
+// max |s| (float bits, atomicMax: order-independent); the diagonal sum is
+// a fixed-order block reduction.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_bj_correct(double2* SR, int n, int Kc, const double* lamK,
+                                                              const double* lamA, unsigned* emax) {
+  const int jc = blockIdx.x;
+  const double top = fabs(lamA[0]);
+  const double noise = BJ_NOISE * top, tiny = 1e-14 * top;
+  const double lj = lamK[jc];
+  double dsum = 0.0;
+  float mx = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (i == jc) continue;
+    const int64_t o = (int64_t)i * 2 * Kc;
+    const double2 xx = SR[o + Kc + jc];
+    const double2 rv = cd(-xx.x, -xx.y);   // R = I - X^H X_K off the diagonal
+    const double li = i < Kc ? lamK[i] : lamA[i];
+    const double2 num = cadd(SR[o + jc], cscale(rv, lj));
+    const double an = cabs_(num);
+    const double den = lj - li;
+    double2 ev;
+    if ((fabs(lj) <= noise && fabs(li) <= noise) || an <= tiny) {
+      // no rotation: a small coupling to first order; otherwise only the
+      // orthonormality between refined columns (an unrefined column's
+      // overlap is its own FP32 error, not a direction to move in)
+      if (an <= tiny && fabs(den) > 100.0 * tiny)
+        ev = cscale(num, 1.0 / den);
+      else
+        ev = i < Kc ? cscale(rv, 0.5) : czero();
+    } else {
+      const double zeta = den / (2.0 * an);
+      const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+      const double c = 1.0 / sqrt(1.0 + t * t);
+      const double sn = c * t;
+      ev = cscale(num, sn / an);
+      dsum -= t * t * c * c / (1.0 + c);   // c - 1
+      mx = fmaxf(mx, (float)fabs(sn));
+    }
+    SR[o + jc] = ev;
+  }
+  double v[1] = {dsum};
+  block_sum<1>(v);
+  if (threadIdx.x == 0) {
+    const int64_t o = (int64_t)jc * 2 * Kc;
+    SR[o + jc] = cd(0.5 * (1.0 - SR[o + Kc + jc].x) + v[0], 0.0);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(emax, __float_as_uint(mx));
+}
+
+// T <- (3 I - T) / 2 (m x m): one Newton-Schulz step's factor.
+__global__ void k_bj_ns(double2* T, int m) {
+  const int64_t total = (int64_t)m * m;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / m), c = (int)(e % m);
+    const double2 t = T[e];
+    T[e] = cd(((r == c ? 3.0 : 0.0) - t.x) * 0.5, -t.y * 0.5);
+  }
+}
+
+// Order of the refined eigenvalues and the rsum2 cutoff: bond c of state b
+// and order[] (the columns of X by descending eigenvalue).  The first Kr
+// columns of X are refined; at most K (<= Kr) are kept.  One block.
+__global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c, int w, int Kr, int K,
+                                                      const double* lamK, const double* stats, int* bonds,
+                                                      int max_bond, double cutoff, int* order, double* lsort) {
+  for (int i = threadIdx.x; i < Kr; i += blockDim.x) {
+    const double li = lamK[i];
+    int rank = 0;
+    for (int j2 = 0; j2 < Kr; ++j2) {
+      const double lj = lamK[j2];
+      rank += (lj > li) || (lj == li && j2 < i);
+    }
+    order[rank] = i;
+    lsort[rank] = li;
   }
   __syncthreads();
   int* bond = bonds + (int64_t)b * (bd.max_n + 1);
   if (threadIdx.x == 0) {
-    int keep = rank_by_cutoff(lam, w, cutoff, max_bond);
+    int keep;
+    if (K == w) {
+      keep = rank_by_cutoff(lsort, w, cutoff, max_bond);
+    } else {
+      // tail_from(i) = trace - sum_{j < i} l_j; keep = the largest i + 1
+      // with tail_from(i) > cutoff * trace, capped at K
+      const double total = stats[1];
+      double head = 0.0;
+      for (int i = 0; i < K; ++i) head += lsort[i] > 0.0 ? lsort[i] : 0.0;
+      keep = 0;
+      if (total - head > cutoff * total) keep = K;
+      for (int i = K - 1; i >= 0 && keep == 0; --i) {
+        head -= lsort[i] > 0.0 ? lsort[i] : 0.0;
+        if (total - head > cutoff * total) keep = i + 1;
+      }
+      if (keep < 1) keep = 1;
+      if (max_bond > 0 && keep > max_bond) keep = max_bond;
+    }
+    if (keep > K) keep = K;
     if (keep > bd.tt_b) keep = bd.tt_b;
     if (c < 30 && keep > (1 << c)) keep = 1 << c;
-    s_keep = keep;
     bond[c] = keep;
   }
+}
+
+// One block per kept column l (order[l] of X): the canonical phase (the
+// pivot rule of phase_fix_column: the lowest row whose magnitude is within
+// QM_PIVOT_TOL of the column's largest, made real positive), the selected
+// column into vsel (stride vstride) and row l of the site tensor of cut c.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, int c, const double2* X, int w,
+                                                           const int* bonds, const int* order, double2* vsel,
+                                                           int vstride, double2* tensors, int chi) {
+  __shared__ double s_m[BLOCK_THREADS / 32];
+  __shared__ int s_j[BLOCK_THREADS / 32];
+  __shared__ double2 s_ph;
+  const int l = blockIdx.x;
+  const int keep = bonds[(int64_t)b * (bd.max_n + 1) + c];
+  if (l >= keep) return;
+  const int col = order[l];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double m = -1.0;
+  for (int i = threadIdx.x; i < w; i += blockDim.x) m = fmax(m, cabs_(X[(int64_t)i * w + col]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) s_m[warp] = m;
   __syncthreads();
-  const int keep = s_keep;
-  for (int col = threadIdx.x; col < keep; col += blockDim.x) phase_fix_column(V, w, w, perm[col]);
+  m = s_m[0];
+  for (int k = 1; k < BLOCK_THREADS / 32; ++k) m = fmax(m, s_m[k]);
+  int jp = w;
+  for (int i = threadIdx.x; i < w; i += blockDim.x)
+    if (cabs_(X[(int64_t)i * w + col]) >= (1.0 - QM_PIVOT_TOL) * m) {
+      jp = i;
+      break;
+    }
+  for (int o = 16; o > 0; o >>= 1) jp = min(jp, __shfl_xor_sync(0xffffffffu, jp, o));
+  if (lane == 0) s_j[warp] = jp;
   __syncthreads();
-  double2* vs = vsel + (int64_t)b * bd.tt_w * bd.tt_w;
-  for (int64_t e = threadIdx.x; e < (int64_t)w * keep; e += blockDim.x) {
-    const int a = (int)(e / keep), col = (int)(e % keep);
-    vs[(int64_t)a * vstride + col] = V[(int64_t)a * w + perm[col]];
+  if (threadIdx.x == 0) {
+    int j = s_j[0];
+    for (int k = 1; k < BLOCK_THREADS / 32; ++k) j = min(j, s_j[k]);
+    if (j >= w) j = 0;
+    const double2 z = X[(int64_t)j * w + col];
+    const double az = cabs_(z);
+    s_ph = az > 0.0 ? cscale(cconj(z), 1.0 / az) : cd(1.0, 0.0);
   }
-  const int r = w / 2;
+  __syncthreads();
+  const double2 ph = s_ph;
+  double2* vs = vsel + (int64_t)b * bd.tt_w * bd.tt_w;
   const int n = bd.n[b];
   const int ce = chi < (1 << (n / 2)) ? chi : (1 << (n / 2));
-  double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce;
-  for (int64_t e = threadIdx.x; e < (int64_t)keep * 2 * r; e += blockDim.x) {
-    const int l = (int)(e / (2 * r)), pr = (int)(e % (2 * r));
-    ts[e] = cconj(V[(int64_t)pr * w + perm[l]]);
+  double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce + (int64_t)l * w;
+  for (int i = threadIdx.x; i < w; i += blockDim.x) {
+    const double2 v = cmul(X[(int64_t)i * w + col], ph);
+    vs[(int64_t)i * vstride + l] = v;
+    ts[i] = cconj(v);
   }
 }
 
@@ -221,48 +724,215 @@ __global__ void __launch_bounds__(256) k_cgemm(const float2* A, int64_t lda, con
   }
 }
 
+
 // ---- host-side drivers -------------------------------------------------------------
 
-// Diagonalise the w x w Gram of state b (in place in `gram`, stride w) with
-// eigenvectors in `vwork`, then finalize cut c.  Synchronises the stream
-// once per sweep.  Returns a cudaError_t.
-int tt_wide_eig(const BatchDev& bd, int b, int c, int w, double2* gram, double2* vwork, WJRot* rot, int* d_count,
-                double* d_trace, int* perm, double* lam, int* bonds, double2* vsel, double2* tensors, int chi,
-                int max_bond, double cutoff, cudaStream_t s) {
-  const int64_t off = (int64_t)b * bd.tt_w * bd.tt_w;
-  double2* G = gram + off;
-  double2* V = vwork + off;
-  const int64_t ww = (int64_t)w * w;
-  int blocks = (int)((ww / 2 + TTW_THREADS - 1) / TTW_THREADS);
-  if (blocks > 152 * 16) blocks = 152 * 16;
+static int bj_round32(int w) { return (w + BJ_S - 1) / BJ_S * BJ_S; }
+
+int bj_alloc(BJScratch& sc, int tt_w, int tt_b) {
+  const int W = bj_round32(tt_w);
+  const int kmax = tt_b + BJ_EXTRA < W ? tt_b + BJ_EXTRA : W;
+  sc.W = W;
+  sc.kmax = kmax;
+  const size_t WW = (size_t)W * W;
+  cudaError_t e = cudaSuccess;
+  auto get = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  get(reinterpret_cast<void**>(&sc.A), sizeof(float2) * WW);
+  get(reinterpret_cast<void**>(&sc.V), sizeof(float2) * WW);
+  get(reinterpret_cast<void**>(&sc.J), sizeof(float2) * (size_t)(W / BJ_S) * BJ_S * BJ_S);
+  get(reinterpret_cast<void**>(&sc.X), sizeof(double2) * WW);
+  get(reinterpret_cast<void**>(&sc.H), sizeof(double2) * WW);
+  get(reinterpret_cast<void**>(&sc.T), sizeof(double2) * WW);
+  get(reinterpret_cast<void**>(&sc.T2), sizeof(double2) * WW);
+  get(reinterpret_cast<void**>(&sc.YX), sizeof(double2) * (size_t)W * 2 * kmax);
+  get(reinterpret_cast<void**>(&sc.SR), sizeof(double2) * (size_t)W * 2 * kmax);
+  get(reinterpret_cast<void**>(&sc.perm), sizeof(int) * W);
+  get(reinterpret_cast<void**>(&sc.order), sizeof(int) * kmax);
+  get(reinterpret_cast<void**>(&sc.count), sizeof(int) * 2);
+  get(reinterpret_cast<void**>(&sc.lamA), sizeof(double) * W);
+  get(reinterpret_cast<void**>(&sc.lamK), sizeof(double) * kmax);
+  get(reinterpret_cast<void**>(&sc.lsort), sizeof(double) * kmax);
+  get(reinterpret_cast<void**>(&sc.stats), sizeof(double) * 4);
+  get(reinterpret_cast<void**>(&sc.part), sizeof(double) * BJ_PARTS);
+  get(reinterpret_cast<void**>(&sc.emax), sizeof(unsigned));
+  return (int)e;
+}
+
+void bj_free(BJScratch& sc) {
+  void* ptrs[] = {sc.A,     sc.V,     sc.J,     sc.X,    sc.H,     sc.T,     sc.T2,   sc.YX,  sc.SR,
+                  sc.perm,  sc.order, sc.count, sc.lamA, sc.lamK, sc.lsort, sc.stats, sc.part, sc.emax};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  sc = BJScratch();
+}
+
+#define BJ_EB (152 * 8)   // grid of the elementwise kernels
+
+static void zgemm(bool conj, const double2* A, int64_t lda, const double2* B, int64_t ldb, const double2* D,
+                  int64_t ldd, double2* C, int64_t ldc, int M, int N, int K, double alpha, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  const dim3 g((M + ZG_T - 1) / ZG_T, (N + ZG_T - 1) / ZG_T);
   qm_note_launch();
-  k_wj_init<<<blocks, TTW_THREADS, 0, s>>>(G, V, w, d_trace);
-  double tr = 0.0;
-  cudaError_t e = cudaMemcpyAsync(&tr, d_trace, sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return (int)e;
-  const double floor_abs = 1e-15 * tr;
-  const int pblocks = (w / 2 + 127) / 128;
-  for (int sweep = 0; sweep < TTW_MAX_SWEEPS; ++sweep) {
-    e = cudaMemsetAsync(d_count, 0, sizeof(int), s);
+  if (conj)
+    k_zgemm<true><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
+  else
+    k_zgemm<false><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
+}
+
+// FP32 blocked Jacobi of the n x n Hermitian H (stride n): eigenvalue order
+// in sc.perm / sc.lamA, the FP64 basis in sc.X (columns in that order),
+// ||H||_F and trace in sc.stats.
+static int bj_fp32(const double2* H, int n, BJScratch& sc, cudaStream_t s, int* sweeps_out) {
+  const int W = bj_round32(n);
+  if (W > sc.W) return (int)cudaErrorInvalidValue;
+  const int nb = W / BJ_B, np = nb / 2;
+  qm_note_launch();
+  k_bj_load<<<BJ_PARTS, BLOCK_THREADS, 0, s>>>(H, n, sc.A, sc.V, W, sc.part);
+  qm_note_launch();
+  k_bj_stats<<<1, BLOCK_THREADS, 0, s>>>(sc.part, BJ_PARTS, H, n, sc.stats);
+  const int nA = np * (np - 1) / 2, nV = (W / BJ_S) * np;
+  int sweeps = 0;
+  for (int sweep = 0; sweep < BJ_MAX_SWEEPS; ++sweep) {
+    cudaError_t e = cudaMemsetAsync(sc.count, 0, sizeof(int), s);
     if (e != cudaSuccess) return (int)e;
-    for (int k = 0; k < w - 1; ++k) {
+    for (int k = 0; k < nb - 1; ++k) {
       qm_note_launch();
-      k_wj_params<<<pblocks, 128, 0, s>>>(G, w, k, floor_abs, rot, d_count);
-      qm_note_launch();
-      k_wj_cols<<<blocks, TTW_THREADS, 0, s>>>(G, V, w, rot);
-      qm_note_launch();
-      k_wj_rows<<<blocks, TTW_THREADS, 0, s>>>(G, w, rot);
+      k_bj_solve<<<np, BJ_THREADS, 0, s>>>(sc.A, W, nb, k, sc.J, sc.stats, sc.count);
+      if (nA + nV > 0) {
+        qm_note_launch();
+        k_bj_update<<<nA + nV, BJ_THREADS, 0, s>>>(sc.A, sc.V, W, nb, k, sc.J, nA);
+      }
     }
+    ++sweeps;
     int cnt = 0;
-    e = cudaMemcpyAsync(&cnt, d_count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(&cnt, sc.count, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return (int)e;
     if (cnt == 0) break;
   }
   qm_note_launch();
-  k_wide_finalize<<<1, 1024, 0, s>>>(bd, b, c, G, V, w, bonds, vsel, bd.tt_b, tensors, chi, max_bond, cutoff, perm,
-                                     lam);
+  k_bj_sort<<<1, 1024, sizeof(float) * W, s>>>(sc.A, W, n, sc.perm, sc.lamA);
+  qm_note_launch();
+  k_bj_basis<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.V, W, n, sc.perm, sc.X);
+  *sweeps_out += sweeps;
+  return (int)cudaGetLastError();
+}
+
+// Ogita-Aishima refinement of the first Kc columns of sc.X (eigenvectors of
+// H, n x n, stride n): on return they are refined in sc.X and their
+// eigenvalues in sc.lamK.
+static int bj_refine(const double2* H, int n, BJScratch& sc, int Kc, double tol, cudaStream_t s, int* steps_out,
+                     float* emax_out) {
+  if (Kc < 1) return 0;
+  if (Kc > sc.kmax) return (int)cudaErrorInvalidValue;
+  double2* Xk = sc.YX + Kc;   // row stride 2 Kc
+  qm_note_launch();
+  k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.X, n, Xk, 2 * Kc, n, Kc);
+  float emax = 0.f;
+  for (int it = 0; it < BJ_MAX_REFINE; ++it) {
+    // Y = H X_K into YX[:, :Kc]; [S | X^H X_K] = X^H YX
+    zgemm(false, H, n, Xk, 2 * Kc, nullptr, 0, sc.YX, 2 * Kc, n, Kc, n, 1.0, s);
+    zgemm(true, sc.X, n, sc.YX, 2 * Kc, nullptr, 0, sc.SR, 2 * Kc, n, 2 * Kc, n, 1.0, s);
+    qm_note_launch();
+    k_bj_lam<<<(Kc + 255) / 256, 256, 0, s>>>(sc.SR, Kc, sc.lamK);
+    cudaError_t e = cudaMemsetAsync(sc.emax, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return (int)e;
+    qm_note_launch();
+    k_bj_correct<<<Kc, BLOCK_THREADS, 0, s>>>(sc.SR, n, Kc, sc.lamK, sc.lamA, sc.emax);
+    // X_K += X E
+    const dim3 g1((n + ZG_T - 1) / ZG_T, (Kc + ZG_T - 1) / ZG_T);
+    qm_note_launch();
+    k_zgemm_small<<<g1, 256, 0, s>>>(sc.X, n, sc.SR, 2 * Kc, Xk, 2 * Kc, n, Kc, n);
+    qm_note_launch();
+    k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(Xk, 2 * Kc, sc.X, n, n, Kc);
+    ++*steps_out;
+    unsigned bits = 0;
+    e = cudaMemcpyAsync(&bits, sc.emax, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int)e;
+    const float prev = emax;
+    std::memcpy(&emax, &bits, sizeof(float));
+    if ((double)emax <= tol) break;
+    if (it > 0 && emax > 0.5f * prev) break;   // no longer converging: the rest is a cluster
+  }
+  if (emax > *emax_out) *emax_out = emax;
+  return (int)cudaGetLastError();
+}
+
+// Diagonalise the w x w Gram of state b (stride w, at b's slot of `gram`)
+// and finalize cut c.  Eigenvalues above BJ_RESOLVED of the largest are
+// resolved by the FP32 sweeps and refined directly.  When the columns that
+// may be kept reach below that (rank-deficient or fast-decaying spectra),
+// the unresolved subspace is projected off the refined columns,
+// re-orthonormalised (one Newton-Schulz step in FP64), and its own Gram
+// X_N^H G X_N, whose scale is that of the small eigenvalues, is solved the
+// same way in `sub`.  Synchronises the stream once per sweep and per
+// refinement step.  Returns a cudaError_t.
+int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, BJScratch& sc, BJScratch& sub,
+                 int* bonds, double2* vsel, double2* tensors, int chi, int max_bond, double cutoff, double refine_tol,
+                 cudaStream_t s, BJStats* st) {
+  const double2* G = gram + (int64_t)b * bd.tt_w * bd.tt_w;
+  int sweeps = 0, steps = 0;
+  float emax = 0.f;
+  int e = bj_fp32(G, w, sc, s, &sweeps);
+  if (e) return e;
+  int K = w;
+  if (max_bond > 0 && K > max_bond) K = max_bond;
+  if (K > bd.tt_b) K = bd.tt_b;
+  if (c < 30 && K > (1 << c)) K = 1 << c;
+  if (K > sc.kmax) return (int)cudaErrorInvalidValue;
+  std::vector<double> lam(w);
+  cudaError_t ce = cudaMemcpyAsync(lam.data(), sc.lamA, sizeof(double) * w, cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return (int)ce;
+  // refined columns: the K that may be kept and the discarded ones whose
+  // FP32 eigenvalue is within BJ_MARGIN of the last kept one (their order
+  // and their mixing with it are below FP32 resolution)
+  int Kr = K;
+  while (Kr < w && Kr < sc.kmax && Kr < K + BJ_EXTRA && lam[Kr] >= lam[K - 1] - BJ_MARGIN * lam[0]) ++Kr;
+  int r = 0;
+  while (r < w && lam[r] > BJ_RESOLVED * lam[0]) ++r;
+  if (Kr <= r || r == 0) {
+    e = bj_refine(G, w, sc, Kr, refine_tol, s, &steps, &emax);
+    if (e) return e;
+  } else {
+    const int m = w - r, K1 = Kr - r;
+    e = bj_refine(G, w, sc, r, refine_tol, s, &steps, &emax);
+    if (e) return e;
+    if (sub.W == 0 && (e = bj_alloc(sub, sc.W, sc.kmax)) != 0) return e;
+    double2* Xn = sc.X + r;   // row stride w
+    // X_N <- X_N - X_R (X_R^H X_N), then one Newton-Schulz step
+    zgemm(true, sc.X, w, Xn, w, nullptr, 0, sc.T, m, r, m, w, 1.0, s);
+    zgemm(false, sc.X, w, sc.T, m, Xn, w, sc.T2, m, w, m, r, -1.0, s);
+    zgemm(true, sc.T2, m, sc.T2, m, nullptr, 0, sc.T, m, m, m, w, 1.0, s);
+    qm_note_launch();
+    k_bj_ns<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T, m);
+    zgemm(false, sc.T2, m, sc.T, m, nullptr, 0, Xn, w, w, m, m, 1.0, s);
+    // Gram of the unresolved subspace, solved in `sub`
+    zgemm(false, G, w, Xn, w, nullptr, 0, sc.T2, m, w, m, w, 1.0, s);
+    zgemm(true, Xn, w, sc.T2, m, nullptr, 0, sub.H, m, m, m, w, 1.0, s);
+    if ((e = bj_fp32(sub.H, m, sub, s, &sweeps)) != 0) return e;
+    if ((e = bj_refine(sub.H, m, sub, K1, refine_tol, s, &steps, &emax)) != 0) return e;
+    // X_N <- X_N U, the refined eigenvalues after those of the resolved part
+    zgemm(false, Xn, w, sub.X, m, nullptr, 0, sc.T2, m, w, m, m, 1.0, s);
+    qm_note_launch();
+    k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T2, m, Xn, w, w, m);
+    ce = cudaMemcpyAsync(sc.lamK + r, sub.lamK, sizeof(double) * K1, cudaMemcpyDeviceToDevice, s);
+    if (ce != cudaSuccess) return (int)ce;
+  }
+  qm_note_launch();
+  k_bj_finalize<<<1, 1024, 0, s>>>(bd, b, c, w, Kr, K, sc.lamK, sc.stats, bonds, max_bond, cutoff, sc.order,
+                                    sc.lsort);
+  qm_note_launch();
+  k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.X, w, bonds, sc.order, vsel, bd.tt_b, tensors, chi);
+  if (st) {
+    st->sweeps += sweeps;
+    st->refine_steps += steps;
+    st->calls += 1;
+    if (emax > st->last_emax) st->last_emax = emax;
+  }
   return (int)cudaGetLastError();
 }
 
@@ -273,5 +943,3 @@ void launch_cgemm(const float2* A, int64_t lda, const double2* B, int64_t ldb, f
   qm_note_launch();
   k_cgemm<<<grid, 256, 0, s>>>(A, lda, B, ldb, C, ldc, M, N, K);
 }
-
-size_t wj_rot_bytes(int w) { return sizeof(WJRot) * (size_t)(w / 2 + 1); }

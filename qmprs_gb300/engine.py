@@ -334,6 +334,15 @@ class Engine:
         self.hd.check(self.lib.qmprs_plan_graph_stats(p.p, ctypes.byref(c), ctypes.byref(r)))
         return c.value, r.value
 
+    def wide_stats(self, p: Plan) -> dict:
+        """Counters of the eigensolver of Grams wider than 128 (bonds above
+        64) in stage (a): Grams solved, FP32 block-Jacobi sweeps, FP64
+        refinement steps, largest first-order correction of a last step."""
+        g, sw, st, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        self.hd.check(self.lib.qmprs_plan_wide_stats(p.p, ctypes.byref(g), ctypes.byref(sw), ctypes.byref(st),
+                                                      ctypes.byref(e)))
+        return {"grams": g.value, "sweeps": sw.value, "refine_steps": st.value, "last_correction": e.value}
+
     def set_profiling(self, p: Plan, on: bool) -> None:
         self.hd.check(self.lib.qmprs_plan_set_profiling(p.p, 1 if on else 0))
 

@@ -31,11 +31,18 @@
 //    E_ij = b / (l_j - l_i), the published step; the full rotation also
 //    resolves near-degenerate pairs), and
 //      X_K <- X_K + X E.
-//    S and R are FP64 products (k_zgemm); the correction X E is small and
-//    taken in FP32 products with an FP64 sum.  A step squares the error, so
+//    S and R are FP64 products (k_zgemm) in the exact mode and double-float
+//    products on the FP32 pipes (k_zgemm_df, about 5x the FP64 rate) in the
+//    fast mode; the correction X E is double-float in the exact mode (the
+//    first corrections reach 0.1-0.5, and FP32 rounding of them would set a
+//    floor near 1e-8) and FP32 in the fast mode.  A step squares the error, so
 //    one or two steps take FP32 eigenvectors to FP64 accuracy; it repeats
 //    until max |E| is below the mode's tolerance, or stops halving (at most
 //    BJ_MAX_REFINE steps).
+//    The columns that stay (beyond K) enter only through their pairs with
+//    the refined ones, whose denominators take their FP64 Rayleigh quotients
+//    (k_bj_rq): the FP32 diagonal is accurate to first order only, which
+//    would slow the convergence to linear.
 //    FP32 resolves eigenvalues down to about 1e-7 of the largest.  When the
 //    columns that may be kept reach below BJ_RESOLVED of it (rank-deficient
 //    Grams, fast-decaying spectra, where the 1e-10 cutoff decides the
@@ -61,13 +68,13 @@
 #include <cstring>
 #include <vector>
 
-#include "device_common.cuh"
+#include "dfloat.cuh"
 
 #define BJ_B 16             // block of indices; a pair of blocks is a subproblem
 #define BJ_S 32             // subproblem size
 #define BJ_THREADS 256
 #define BJ_MAX_SWEEPS 24
-#define BJ_MAX_REFINE 4
+#define BJ_MAX_REFINE 6
 #define BJ_PARTS 256        // blocks of the norm reduction (fixed: deterministic sums)
 #define BJ_NOISE 1e-6       // eigenvalues below this fraction of the largest are FP32 noise
 #define BJ_MARGIN 1e-5      // discarded columns this close (of the largest) to the last kept one ...
@@ -145,95 +152,108 @@ __global__ void k_bj_stats(const double* part, int nparts, const double2* G, int
   }
 }
 
+// Rotation of pair (p, q) of the 32 x 32 subproblem m: c, s e and s conj(e)
+// (the Rutishauser-style stable rotation that zeroes m[p][q]); flag 0 when
+// |m[p][q]| is below FP32 resolution (1e-7 relative, or floor_abs), big 1
+// when it is above 1e-5 relative (the sweep has not converged).
+struct BJRot {
+  float c;
+  float2 se, sce;
+  int flag, big;
+};
+__device__ __forceinline__ BJRot bj_rot(const float2 (*m)[BJ_S + 1], int p, int q, float floor_abs, float big_abs) {
+  BJRot r;
+  const float2 g = m[p][q];
+  const float ag = sqrtf(g.x * g.x + g.y * g.y);
+  const float app = m[p][p].x, aqq = m[q][q].x;
+  const float scale = sqrtf(fabsf(app * aqq));
+  r.flag = ag > floor_abs && ag > 1e-7f * scale;
+  r.big = r.flag && ag > 1e-5f * scale && ag > big_abs;
+  r.c = 1.f;
+  r.se = r.sce = cf(0.f, 0.f);
+  if (r.flag) {
+    const float zeta = (aqq - app) / (2.f * ag);
+    const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+    const float c = 1.f / sqrtf(1.f + t * t);
+    const float sg = c * t / ag;
+    r.c = c;
+    r.se = cf(g.x * sg, g.y * sg);
+    r.sce = cf(g.x * sg, -g.y * sg);
+  }
+  return r;
+}
+
 // One block per pair of round k: one Jacobi sweep of the 32 x 32
 // subproblem; J (32 x 32, row-major) to Jbuf[pair]; the rotated diagonal
-// tile back into A.  count += rotations above 1e-5 relative.
+// tile back into A.  count += 1 if a rotation was above 1e-5 relative.
+// Thread (gr, gc) owns the 2 x 2 entry group of inner pairs (gr, gc) and
+// computes both rotations itself; the subproblem is double-buffered (read
+// one copy, write the other), so an inner round takes one barrier.
 __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int nb, int k, float2* Jbuf,
                                                          const double* stats, int* count) {
-  __shared__ float2 a[BJ_S][BJ_S + 1];
+  __shared__ float2 a[2][BJ_S][BJ_S + 1];
   __shared__ float2 j[BJ_S][BJ_S + 1];
-  __shared__ float rc[BJ_S / 2];
-  __shared__ float2 rse[BJ_S / 2], rsce[BJ_S / 2];
-  __shared__ int rflag[BJ_S / 2];
   __shared__ int s_big;
   const int pair = blockIdx.x, tid = threadIdx.x;
   if (tid == 0) s_big = 0;
   for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
     const int r = e / BJ_S, c = e % BJ_S;
-    a[r][c] = A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)];
+    a[0][r][c] = A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)];
     j[r][c] = cf(r == c ? 1.f : 0.f, 0.f);
   }
-  const float floor_abs = 1e-7f * (float)stats[0];
+  const float floor_abs = 1e-7f * (float)stats[0], big_abs = 1e-6f * (float)stats[0];
   __syncthreads();
-  // 2 x 2 entry group of this thread: pairs (gr, gc) of the inner round
   const int gr = tid / (BJ_S / 2), gc = tid % (BJ_S / 2);
+  int big = 0;
   for (int ir = 0; ir < BJ_S - 1; ++ir) {
-    if (tid < BJ_S / 2) {
-      int p, q;
-      bj_pair(BJ_S, ir, tid, &p, &q);
-      const float2 g = a[p][q];
-      const float ag = hypotf(g.x, g.y);
-      const float app = a[p][p].x, aqq = a[q][q].x;
-      const float scale = sqrtf(fabsf(app * aqq));
-      const int flag = ag > floor_abs && ag > 1e-7f * scale;
-      rflag[tid] = flag;
-      if (flag) {
-        const float zeta = (aqq - app) / (2.f * ag);
-        const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-        const float c = 1.f / sqrtf(1.f + t * t);
-        const float s = c * t;
-        const float2 e = cf(g.x / ag, g.y / ag);
-        rc[tid] = c;
-        rse[tid] = cf(e.x * s, e.y * s);
-        rsce[tid] = cf(e.x * s, -e.y * s);
-        if (ag > 1e-5f * scale && ag > 1e-6f * (float)stats[0]) s_big = 1;
-      }
+    const float2 (*cur)[BJ_S + 1] = a[ir & 1];
+    float2 (*nxt)[BJ_S + 1] = a[(ir + 1) & 1];
+    int pr, qr, pc, qc;
+    bj_pair(BJ_S, ir, gr, &pr, &qr);
+    bj_pair(BJ_S, ir, gc, &pc, &qc);
+    const BJRot rr = bj_rot(cur, pr, qr, floor_abs, big_abs);
+    const BJRot rcl = gr == gc ? rr : bj_rot(cur, pc, qc, floor_abs, big_abs);
+    big |= rcl.big;
+    float2 x00 = cur[pr][pc], x01 = cur[pr][qc], x10 = cur[qr][pc], x11 = cur[qr][qc];
+    if (rcl.flag) {   // columns: col_p <- c col_p - s conj(e) col_q ; col_q <- s e col_p + c col_q
+      const float c = rcl.c;
+      const float2 se = rcl.se, sce = rcl.sce;
+      const float2 n00 = cf(c * x00.x - (sce.x * x01.x - sce.y * x01.y), c * x00.y - (sce.x * x01.y + sce.y * x01.x));
+      const float2 n01 = cf(se.x * x00.x - se.y * x00.y + c * x01.x, se.x * x00.y + se.y * x00.x + c * x01.y);
+      const float2 n10 = cf(c * x10.x - (sce.x * x11.x - sce.y * x11.y), c * x10.y - (sce.x * x11.y + sce.y * x11.x));
+      const float2 n11 = cf(se.x * x10.x - se.y * x10.y + c * x11.x, se.x * x10.y + se.y * x10.x + c * x11.y);
+      x00 = n00;
+      x01 = n01;
+      x10 = n10;
+      x11 = n11;
     }
-    __syncthreads();
-    {
-      int pr, qr, pc, qc;
-      bj_pair(BJ_S, ir, gr, &pr, &qr);
-      bj_pair(BJ_S, ir, gc, &pc, &qc);
-      float2 x00 = a[pr][pc], x01 = a[pr][qc], x10 = a[qr][pc], x11 = a[qr][qc];
-      if (rflag[gc]) {   // columns: col_p <- c col_p - s conj(e) col_q ; col_q <- s e col_p + c col_q
-        const float c = rc[gc];
-        const float2 se = rse[gc], sce = rsce[gc];
-        const float2 n00 = cf(c * x00.x - (sce.x * x01.x - sce.y * x01.y), c * x00.y - (sce.x * x01.y + sce.y * x01.x));
-        const float2 n01 = cf(se.x * x00.x - se.y * x00.y + c * x01.x, se.x * x00.y + se.y * x00.x + c * x01.y);
-        const float2 n10 = cf(c * x10.x - (sce.x * x11.x - sce.y * x11.y), c * x10.y - (sce.x * x11.y + sce.y * x11.x));
-        const float2 n11 = cf(se.x * x10.x - se.y * x10.y + c * x11.x, se.x * x10.y + se.y * x10.x + c * x11.y);
-        x00 = n00;
-        x01 = n01;
-        x10 = n10;
-        x11 = n11;
-      }
-      if (rflag[gr]) {   // rows: row_p <- c row_p - s e row_q ; row_q <- s conj(e) row_p + c row_q
-        const float c = rc[gr];
-        const float2 se = rse[gr], sce = rsce[gr];
-        const float2 n00 = cf(c * x00.x - (se.x * x10.x - se.y * x10.y), c * x00.y - (se.x * x10.y + se.y * x10.x));
-        const float2 n01 = cf(c * x01.x - (se.x * x11.x - se.y * x11.y), c * x01.y - (se.x * x11.y + se.y * x11.x));
-        const float2 n10 = cf(sce.x * x00.x - sce.y * x00.y + c * x10.x, sce.x * x00.y + sce.y * x00.x + c * x10.y);
-        const float2 n11 = cf(sce.x * x01.x - sce.y * x01.y + c * x11.x, sce.x * x01.y + sce.y * x01.x + c * x11.y);
-        x00 = n00;
-        x01 = n01;
-        x10 = n10;
-        x11 = n11;
-      }
-      if (gr == gc) {    // the rotated pair: real diagonal, eliminated off-diagonal
-        x00.y = 0.f;
-        x11.y = 0.f;
-        if (rflag[gr]) x01 = x10 = cf(0.f, 0.f);
-      }
-      a[pr][pc] = x00;
-      a[pr][qc] = x01;
-      a[qr][pc] = x10;
-      a[qr][qc] = x11;
-      // J <- J R on the columns of pair (tid % 16), rows tid / 16 and tid / 16 + 16
+    if (rr.flag) {    // rows: row_p <- c row_p - s e row_q ; row_q <- s conj(e) row_p + c row_q
+      const float c = rr.c;
+      const float2 se = rr.se, sce = rr.sce;
+      const float2 n00 = cf(c * x00.x - (se.x * x10.x - se.y * x10.y), c * x00.y - (se.x * x10.y + se.y * x10.x));
+      const float2 n01 = cf(c * x01.x - (se.x * x11.x - se.y * x11.y), c * x01.y - (se.x * x11.y + se.y * x11.x));
+      const float2 n10 = cf(sce.x * x00.x - sce.y * x00.y + c * x10.x, sce.x * x00.y + sce.y * x00.x + c * x10.y);
+      const float2 n11 = cf(sce.x * x01.x - sce.y * x01.y + c * x11.x, sce.x * x01.y + sce.y * x01.x + c * x11.y);
+      x00 = n00;
+      x01 = n01;
+      x10 = n10;
+      x11 = n11;
+    }
+    if (gr == gc) {   // the rotated pair: real diagonal, eliminated off-diagonal
+      x00.y = 0.f;
+      x11.y = 0.f;
+      if (rr.flag) x01 = x10 = cf(0.f, 0.f);
+    }
+    nxt[pr][pc] = x00;
+    nxt[pr][qc] = x01;
+    nxt[qr][pc] = x10;
+    nxt[qr][qc] = x11;
+    // J <- J R on the columns of pair gc, rows gr and gr + 16 (one owner each)
+    if (rcl.flag) {
+      const float c = rcl.c;
+      const float2 se = rcl.se, sce = rcl.sce;
       for (int h = 0; h < 2; ++h) {
         const int row = gr + h * (BJ_S / 2);
-        if (!rflag[gc]) continue;
-        const float c = rc[gc];
-        const float2 se = rse[gc], sce = rsce[gc];
         const float2 vp = j[row][pc], vq = j[row][qc];
         j[row][pc] = cf(c * vp.x - (sce.x * vq.x - sce.y * vq.y), c * vp.y - (sce.x * vq.y + sce.y * vq.x));
         j[row][qc] = cf(se.x * vp.x - se.y * vp.y + c * vq.x, se.x * vp.y + se.y * vp.x + c * vq.y);
@@ -241,43 +261,73 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
     }
     __syncthreads();
   }
+  if (big) s_big = 1;
+  const float2 (*fin)[BJ_S + 1] = a[(BJ_S - 1) & 1];
   float2* jo = Jbuf + (int64_t)pair * BJ_S * BJ_S;
   for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
     const int r = e / BJ_S, c = e % BJ_S;
     jo[e] = j[r][c];
     // Hermitian diagonal tile: the upper triangle and its mirror
-    const float2 v = r <= c ? a[r][c] : cf(a[c][r].x, -a[c][r].y);
+    const float2 v = r <= c ? fin[r][c] : cf(fin[c][r].x, -fin[c][r].y);
     A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)] = v;
   }
+  __syncthreads();
   if (tid == 0 && s_big) atomicAdd(count, 1);
 }
 
-// 32 x 32 complex product in shared memory, 4 consecutive outputs per
-// thread (row tid / 8, columns 4 (tid % 8) ...): out = (CONJ ? x^H : x) y.
+// 32 x 32 complex products of k_bj_update in shared memory (rows padded to
+// 34 entries: 16-byte aligned pairs, distinct banks for the 4 rows a warp
+// reads): 128 threads, a 4 x 2 block of outputs each (rows 4 (tid / 16) ..,
+// columns 2 (tid % 16) ..); out = (CONJ ? x^H : x) y.
+#define BJU_THREADS 128
+#define BJU_LD (BJ_S + 2)
 template <bool CONJ>
-__device__ __forceinline__ void bj_mm32(const float2 (*x)[BJ_S + 1], const float2 (*y)[BJ_S + 1], float2 (&out)[4]) {
-  const int r = threadIdx.x / 8, c0 = (threadIdx.x % 8) * 4;
+__device__ __forceinline__ void bj_mm32(const float2 (*x)[BJU_LD], const float2 (*y)[BJU_LD], float2 (&out)[4][2]) {
+  const int r0 = (threadIdx.x / 16) * 4, c0 = (threadIdx.x % 16) * 2;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) out[i] = cf(0.f, 0.f);
-#pragma unroll 8
+  for (int i = 0; i < 4; ++i) out[i][0] = out[i][1] = cf(0.f, 0.f);
+#pragma unroll 4
   for (int m = 0; m < BJ_S; ++m) {
-    const float2 xv = CONJ ? x[m][r] : x[r][m];
+    float2 xv[4];
+    if (CONJ) {
+      const float4 a = *reinterpret_cast<const float4*>(&x[m][r0]);
+      const float4 b = *reinterpret_cast<const float4*>(&x[m][r0 + 2]);
+      xv[0] = cf(a.x, a.y);
+      xv[1] = cf(a.z, a.w);
+      xv[2] = cf(b.x, b.y);
+      xv[3] = cf(b.z, b.w);
+    } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) out[i] = CONJ ? fcfmac(out[i], xv, y[m][c0 + i]) : fcfma(out[i], xv, y[m][c0 + i]);
+      for (int i = 0; i < 4; ++i) xv[i] = x[r0 + i][m];
+    }
+    const float4 yy = *reinterpret_cast<const float4*>(&y[m][c0]);
+    const float2 y0 = cf(yy.x, yy.y), y1 = cf(yy.z, yy.w);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      out[i][0] = CONJ ? fcfmac(out[i][0], xv[i], y0) : fcfma(out[i][0], xv[i], y0);
+      out[i][1] = CONJ ? fcfmac(out[i][1], xv[i], y1) : fcfma(out[i][1], xv[i], y1);
+    }
   }
 }
 
+__device__ __forceinline__ void bj_store32(float2 (*t)[BJU_LD], const float2 (&out)[4][2]) {
+  const int r0 = (threadIdx.x / 16) * 4, c0 = (threadIdx.x % 16) * 2;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) *reinterpret_cast<float4*>(&t[r0 + i][c0]) = make_float4(out[i][0].x, out[i][0].y,
+                                                                                        out[i][1].x, out[i][1].y);
+}
+
 // Blocks [0, nA): off-diagonal tiles P < Q of round k (upper triangle in
-// row order), A[P,Q] <- J_P^H A[P,Q] J_Q and its mirror; blocks [nA, nA +
-// nV): V[R rows, Q] <- V[R rows, Q] J_Q for row tiles R of 32 rows.
-__global__ void __launch_bounds__(BJ_THREADS) k_bj_update(float2* A, float2* V, int W, int nb, int k,
-                                                          const float2* Jbuf, int nA) {
-  __shared__ float2 t[BJ_S][BJ_S + 1];
-  __shared__ float2 jq[BJ_S][BJ_S + 1];
-  __shared__ float2 jp[BJ_S][BJ_S + 1];
+// row order), A[P,Q] <- J_P^H A[P,Q] J_Q and its mirror (both written row
+// by row from shared memory); blocks [nA, nA + nV): V[R rows, Q] <-
+// V[R rows, Q] J_Q for row tiles R of 32 rows.
+__global__ void __launch_bounds__(BJU_THREADS) k_bj_update(float2* A, float2* V, int W, int nb, int k,
+                                                           const float2* Jbuf, int nA) {
+  __shared__ __align__(16) float2 t[BJ_S][BJU_LD];
+  __shared__ __align__(16) float2 jq[BJ_S][BJU_LD];
+  __shared__ __align__(16) float2 jp[BJ_S][BJU_LD];
   const int np = nb / 2, tid = threadIdx.x;
-  const int r = tid / 8, c0 = (tid % 8) * 4;
-  float2 out[4];
+  float2 out[4][2];
   if ((int)blockIdx.x < nA) {
     // tile index -> (P, Q), P < Q: row P holds np - 1 - P tiles
     int rem = blockIdx.x, P = 0;
@@ -295,16 +345,17 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_update(float2* A, float2* V, 
     __syncthreads();
     bj_mm32<false>(t, jq, out);   // U = T J_Q
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 4; ++i) t[r][c0 + i] = out[i];
+    bj_store32(t, out);
     __syncthreads();
     bj_mm32<true>(jp, t, out);    // J_P^H U
-    const int gi = bj_index(nb, k, P, r);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int gj = bj_index(nb, k, Q, c0 + i);
-      A[(int64_t)gi * W + gj] = out[i];
-      A[(int64_t)gj * W + gi] = cf(out[i].x, -out[i].y);
+    __syncthreads();
+    bj_store32(t, out);
+    __syncthreads();
+    for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+      const int rr = e / BJ_S, cc = e % BJ_S;
+      A[(int64_t)bj_index(nb, k, P, rr) * W + bj_index(nb, k, Q, cc)] = t[rr][cc];
+      const float2 v = t[cc][rr];
+      A[(int64_t)bj_index(nb, k, Q, rr) * W + bj_index(nb, k, P, cc)] = cf(v.x, -v.y);
     }
   } else {
     const int tI = blockIdx.x - nA;
@@ -316,8 +367,13 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_update(float2* A, float2* V, 
     }
     __syncthreads();
     bj_mm32<false>(t, jq, out);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) V[(int64_t)(R * BJ_S + r) * W + bj_index(nb, k, Q, c0 + i)] = out[i];
+    __syncthreads();
+    bj_store32(t, out);
+    __syncthreads();
+    for (int e = tid; e < BJ_S * BJ_S; e += blockDim.x) {
+      const int rr = e / BJ_S, cc = e % BJ_S;
+      V[(int64_t)(R * BJ_S + rr) * W + bj_index(nb, k, Q, cc)] = t[rr][cc];
+    }
   }
 }
 
@@ -421,20 +477,90 @@ __global__ void __launch_bounds__(256) k_zgemm(const double2* A, int64_t lda, co
   }
 }
 
-// C += A B with a small B (the correction X E): FP32 products (exact in FP64
-// after rounding both factors to FP32), FP32 sums over chunks of 8, FP64
-// sums over chunks.  Same tiling as k_zgemm.
+// The same product in double-float on the FP32 pipes (dfloat.cuh): both
+// factors split into FP32 hi + lo on load, exact high products, TwoSum
+// accumulation; about 2^-46 per operation, 1e-13 of the summed magnitudes
+// over K = 2048 terms, at about 5x the FP64 rate.
+template <bool CONJ>
+__global__ void __launch_bounds__(256) k_zgemm_df(const double2* A, int64_t lda, const double2* B, int64_t ldb,
+                                                  const double2* D, int64_t ldd, double2* C, int64_t ldc, int M,
+                                                  int N, int K, double alpha) {
+  __shared__ xc As[ZG_K][ZG_T + 1];
+  __shared__ xc Bs[ZG_K][ZG_T];
+  const int m0 = blockIdx.x * ZG_T, n0 = blockIdx.y * ZG_T;
+  const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+  XA acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = xa_zero();
+  for (int k0 = 0; k0 < K; k0 += ZG_K) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < ZG_T * ZG_K; e += blockDim.x) {
+      int mm, kk;
+      if (CONJ) {
+        kk = e / ZG_T;
+        mm = e % ZG_T;
+      } else {
+        mm = e / ZG_K;
+        kk = e % ZG_K;
+      }
+      const int gm = m0 + mm, gk = k0 + kk;
+      double2 v = czero();
+      if (gm < M && gk < K) v = CONJ ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk];
+      As[kk][mm] = xc_from_d(v);
+      const int kb = e / ZG_T, nn = e % ZG_T;
+      const int gkb = k0 + kb, gn = n0 + nn;
+      Bs[kb][nn] = xc_from_d((gkb < K && gn < N) ? B[(int64_t)gkb * ldb + gn] : czero());
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < ZG_K; ++kk) {
+      xc av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][tr * 4 + i];
+#pragma unroll
+      for (int j2 = 0; j2 < 4; ++j2) bv[j2] = Bs[kk][tc * 4 + j2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j2 = 0; j2 < 4; ++j2) {
+          if (CONJ)
+            xa_macc(acc[i][j2], av[i], bv[j2]);
+          else
+            xa_mac(acc[i][j2], av[i], bv[j2]);
+        }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tr * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j2 = 0; j2 < 4; ++j2) {
+      const int gn = n0 + tc * 4 + j2;
+      if (gn >= N) continue;
+      double2 v = cscale(xa_to_d(acc[i][j2]), alpha);
+      if (D) v = cadd(v, D[(int64_t)gm * ldd + gn]);
+      C[(int64_t)gm * ldc + gn] = v;
+    }
+  }
+}
+
+// C += A B with a small B (the fast mode's correction X E): FP32 products
+// and sums (|X E| is at most the mode's tolerance, so the rounding is below
+// 1e-10).  Same tiling as k_zgemm.
 __global__ void __launch_bounds__(256) k_zgemm_small(const double2* A, int64_t lda, const double2* B, int64_t ldb,
                                                      double2* C, int64_t ldc, int M, int N, int K) {
   __shared__ float2 As[ZG_K][ZG_T + 1];
   __shared__ float2 Bs[ZG_K][ZG_T];
   const int m0 = blockIdx.x * ZG_T, n0 = blockIdx.y * ZG_T;
   const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
-  double2 acc[4][4];
+  float2 part[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = czero();
+    for (int j2 = 0; j2 < 4; ++j2) part[i][j2] = cf(0.f, 0.f);
   for (int k0 = 0; k0 < K; k0 += ZG_K) {
     __syncthreads();
     for (int e = threadIdx.x; e < ZG_T * ZG_K; e += blockDim.x) {
@@ -448,11 +574,6 @@ __global__ void __launch_bounds__(256) k_zgemm_small(const double2* A, int64_t l
       Bs[kb][nn] = cf((float)u.x, (float)u.y);
     }
     __syncthreads();
-    float2 part[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j2 = 0; j2 < 4; ++j2) part[i][j2] = cf(0.f, 0.f);
 #pragma unroll
     for (int kk = 0; kk < ZG_K; ++kk) {
       float2 av[4], bv[4];
@@ -465,10 +586,6 @@ __global__ void __launch_bounds__(256) k_zgemm_small(const double2* A, int64_t l
 #pragma unroll
         for (int j2 = 0; j2 < 4; ++j2) part[i][j2] = fcfma(part[i][j2], av[i], bv[j2]);
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j2 = 0; j2 < 4; ++j2) acc[i][j2] = cadd(acc[i][j2], f2d(part[i][j2]));
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -477,7 +594,7 @@ __global__ void __launch_bounds__(256) k_zgemm_small(const double2* A, int64_t l
 #pragma unroll
     for (int j2 = 0; j2 < 4; ++j2) {
       const int gn = n0 + tc * 4 + j2;
-      if (gn < N) C[(int64_t)gm * ldc + gn] = cadd(C[(int64_t)gm * ldc + gn], acc[i][j2]);
+      if (gn < N) C[(int64_t)gm * ldc + gn] = cadd(C[(int64_t)gm * ldc + gn], f2d(part[i][j2]));
     }
   }
 }
@@ -506,17 +623,17 @@ __global__ void k_bj_lam(const double2* SR, int Kc, double* lamK) {
 // and cos - 1 into E_jj, next to R_jj / 2.  For a small coupling s e is
 // the first-order b / (l_j - l_i); near-degenerate pairs get the full
 // rotation.  Pairs of eigenvalues both below BJ_NOISE of the largest
-// (lamA[0], below the FP32 sweeps' resolution) and couplings at FP64
-// rounding level take no rotation: between two refined columns they only
+// (lamA[0], below the FP32 sweeps' resolution) and couplings at the
+// rounding level of the products (tiny_rel of the largest) take no rotation: between two refined columns they only
 // restore orthonormality (E_ij = R_ij / 2), against an unrefined column
 // nothing (its overlap is that column's own FP32 error).  emax =
 // max |s| (float bits, atomicMax: order-independent); the diagonal sum is
 // a fixed-order block reduction.
 __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_correct(double2* SR, int n, int Kc, const double* lamK,
-                                                              const double* lamA, unsigned* emax) {
+                                                              const double* lamA, double tiny_rel, unsigned* emax) {
   const int jc = blockIdx.x;
   const double top = fabs(lamA[0]);
-  const double noise = BJ_NOISE * top, tiny = 1e-14 * top;
+  const double noise = BJ_NOISE * top, tiny = tiny_rel * top;
   const double lj = lamK[jc];
   double dsum = 0.0;
   float mx = 0.f;
@@ -557,6 +674,25 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_correct(double2* SR, int n
   }
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(emax, __float_as_uint(mx));
+}
+
+// Rayleigh quotients of the columns c0 .. n-1 of X (n x n, stride n) that
+// the refinement does not move: lamA[i] = Re(x_i^H (H x_i)) / |x_i|^2 with
+// H x_i in T (column i - c0, stride ldt).  They are the denominators of
+// those columns' pairs, accurate to second order in the FP32 eigenvectors'
+// error where the FP32 diagonal is accurate only to first order.  One block
+// per column, fixed-order reduction.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_bj_rq(const double2* X, int n, const double2* T, int ldt, int c0,
+                                                         double* lamA) {
+  const int i = c0 + blockIdx.x;
+  double v[2] = {0.0, 0.0};
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double2 x = X[(int64_t)k * n + i], t = T[(int64_t)k * ldt + (i - c0)];
+    v[0] += x.x * t.x + x.y * t.y;
+    v[1] += x.x * x.x + x.y * x.y;
+  }
+  block_sum<2>(v);
+  if (threadIdx.x == 0) lamA[i] = v[1] > 0.0 ? v[0] / v[1] : 0.0;
 }
 
 // T <- (3 I - T) / 2 (m x m): one Newton-Schulz step's factor.
@@ -770,15 +906,23 @@ void bj_free(BJScratch& sc) {
 
 #define BJ_EB (152 * 8)   // grid of the elementwise kernels
 
+// FP64 products (df = false) or double-float (df = true)
 static void zgemm(bool conj, const double2* A, int64_t lda, const double2* B, int64_t ldb, const double2* D,
-                  int64_t ldd, double2* C, int64_t ldc, int M, int N, int K, double alpha, cudaStream_t s) {
+                  int64_t ldd, double2* C, int64_t ldc, int M, int N, int K, double alpha, cudaStream_t s,
+                  bool df = false) {
   if (M <= 0 || N <= 0) return;
   const dim3 g((M + ZG_T - 1) / ZG_T, (N + ZG_T - 1) / ZG_T);
   qm_note_launch();
-  if (conj)
+  if (df) {
+    if (conj)
+      k_zgemm_df<true><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
+    else
+      k_zgemm_df<false><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
+  } else if (conj) {
     k_zgemm<true><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
-  else
+  } else {
     k_zgemm<false><<<g, 256, 0, s>>>(A, lda, B, ldb, D, ldd, C, ldc, M, N, K, alpha);
+  }
 }
 
 // FP32 blocked Jacobi of the n x n Hermitian H (stride n): eigenvalue order
@@ -802,7 +946,7 @@ static int bj_fp32(const double2* H, int n, BJScratch& sc, cudaStream_t s, int* 
       k_bj_solve<<<np, BJ_THREADS, 0, s>>>(sc.A, W, nb, k, sc.J, sc.stats, sc.count);
       if (nA + nV > 0) {
         qm_note_launch();
-        k_bj_update<<<nA + nV, BJ_THREADS, 0, s>>>(sc.A, sc.V, W, nb, k, sc.J, nA);
+        k_bj_update<<<nA + nV, BJU_THREADS, 0, s>>>(sc.A, sc.V, W, nb, k, sc.J, nA);
       }
     }
     ++sweeps;
@@ -823,28 +967,37 @@ static int bj_fp32(const double2* H, int n, BJScratch& sc, cudaStream_t s, int* 
 // Ogita-Aishima refinement of the first Kc columns of sc.X (eigenvectors of
 // H, n x n, stride n): on return they are refined in sc.X and their
 // eigenvalues in sc.lamK.
-static int bj_refine(const double2* H, int n, BJScratch& sc, int Kc, double tol, cudaStream_t s, int* steps_out,
-                     float* emax_out) {
+static int bj_refine(const double2* H, int n, BJScratch& sc, int Kc, double tol, bool df, cudaStream_t s,
+                     int* steps_out, float* emax_out) {
   if (Kc < 1) return 0;
   if (Kc > sc.kmax) return (int)cudaErrorInvalidValue;
+  if (Kc < n) {   // eigenvalue estimates of the columns that stay
+    zgemm(false, H, n, sc.X + Kc, n, nullptr, 0, sc.T2, n - Kc, n, n - Kc, n, 1.0, s, df);
+    qm_note_launch();
+    k_bj_rq<<<n - Kc, BLOCK_THREADS, 0, s>>>(sc.X, n, sc.T2, n - Kc, Kc, sc.lamA);
+  }
   double2* Xk = sc.YX + Kc;   // row stride 2 Kc
   qm_note_launch();
   k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.X, n, Xk, 2 * Kc, n, Kc);
   float emax = 0.f;
   for (int it = 0; it < BJ_MAX_REFINE; ++it) {
     // Y = H X_K into YX[:, :Kc]; [S | X^H X_K] = X^H YX
-    zgemm(false, H, n, Xk, 2 * Kc, nullptr, 0, sc.YX, 2 * Kc, n, Kc, n, 1.0, s);
-    zgemm(true, sc.X, n, sc.YX, 2 * Kc, nullptr, 0, sc.SR, 2 * Kc, n, 2 * Kc, n, 1.0, s);
+    zgemm(false, H, n, Xk, 2 * Kc, nullptr, 0, sc.YX, 2 * Kc, n, Kc, n, 1.0, s, df);
+    zgemm(true, sc.X, n, sc.YX, 2 * Kc, nullptr, 0, sc.SR, 2 * Kc, n, 2 * Kc, n, 1.0, s, df);
     qm_note_launch();
     k_bj_lam<<<(Kc + 255) / 256, 256, 0, s>>>(sc.SR, Kc, sc.lamK);
     cudaError_t e = cudaMemsetAsync(sc.emax, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return (int)e;
     qm_note_launch();
-    k_bj_correct<<<Kc, BLOCK_THREADS, 0, s>>>(sc.SR, n, Kc, sc.lamK, sc.lamA, sc.emax);
+    k_bj_correct<<<Kc, BLOCK_THREADS, 0, s>>>(sc.SR, n, Kc, sc.lamK, sc.lamA, df ? 1e-12 : 1e-14, sc.emax);
     // X_K += X E
     const dim3 g1((n + ZG_T - 1) / ZG_T, (Kc + ZG_T - 1) / ZG_T);
     qm_note_launch();
-    k_zgemm_small<<<g1, 256, 0, s>>>(sc.X, n, sc.SR, 2 * Kc, Xk, 2 * Kc, n, Kc, n);
+    if (df) {
+      k_zgemm_small<<<g1, 256, 0, s>>>(sc.X, n, sc.SR, 2 * Kc, Xk, 2 * Kc, n, Kc, n);
+    } else {   // the exact mode: large first corrections need their own low-order bits
+      k_zgemm_df<false><<<g1, 256, 0, s>>>(sc.X, n, sc.SR, 2 * Kc, Xk, 2 * Kc, Xk, 2 * Kc, n, Kc, n, 1.0);
+    }
     qm_note_launch();
     k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(Xk, 2 * Kc, sc.X, n, n, Kc);
     ++*steps_out;
@@ -874,6 +1027,9 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, B
                  int* bonds, double2* vsel, double2* tensors, int chi, int max_bond, double cutoff, double refine_tol,
                  cudaStream_t s, BJStats* st) {
   const double2* G = gram + (int64_t)b * bd.tt_w * bd.tt_w;
+  // the fast mode's tolerance leaves about 1e-8 of error: double-float
+  // refinement products suffice there; the exact mode takes FP64 products
+  const bool df = refine_tol > BJ_TOL_EXACT;
   int sweeps = 0, steps = 0;
   float emax = 0.f;
   int e = bj_fp32(G, w, sc, s, &sweeps);
@@ -895,28 +1051,28 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, B
   int r = 0;
   while (r < w && lam[r] > BJ_RESOLVED * lam[0]) ++r;
   if (Kr <= r || r == 0) {
-    e = bj_refine(G, w, sc, Kr, refine_tol, s, &steps, &emax);
+    e = bj_refine(G, w, sc, Kr, refine_tol, df, s, &steps, &emax);
     if (e) return e;
   } else {
     const int m = w - r, K1 = Kr - r;
-    e = bj_refine(G, w, sc, r, refine_tol, s, &steps, &emax);
+    e = bj_refine(G, w, sc, r, refine_tol, df, s, &steps, &emax);
     if (e) return e;
     if (sub.W == 0 && (e = bj_alloc(sub, sc.W, sc.kmax)) != 0) return e;
     double2* Xn = sc.X + r;   // row stride w
     // X_N <- X_N - X_R (X_R^H X_N), then one Newton-Schulz step
-    zgemm(true, sc.X, w, Xn, w, nullptr, 0, sc.T, m, r, m, w, 1.0, s);
-    zgemm(false, sc.X, w, sc.T, m, Xn, w, sc.T2, m, w, m, r, -1.0, s);
-    zgemm(true, sc.T2, m, sc.T2, m, nullptr, 0, sc.T, m, m, m, w, 1.0, s);
+    zgemm(true, sc.X, w, Xn, w, nullptr, 0, sc.T, m, r, m, w, 1.0, s, df);
+    zgemm(false, sc.X, w, sc.T, m, Xn, w, sc.T2, m, w, m, r, -1.0, s, df);
+    zgemm(true, sc.T2, m, sc.T2, m, nullptr, 0, sc.T, m, m, m, w, 1.0, s, df);
     qm_note_launch();
     k_bj_ns<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T, m);
-    zgemm(false, sc.T2, m, sc.T, m, nullptr, 0, Xn, w, w, m, m, 1.0, s);
+    zgemm(false, sc.T2, m, sc.T, m, nullptr, 0, Xn, w, w, m, m, 1.0, s, df);
     // Gram of the unresolved subspace, solved in `sub`
-    zgemm(false, G, w, Xn, w, nullptr, 0, sc.T2, m, w, m, w, 1.0, s);
-    zgemm(true, Xn, w, sc.T2, m, nullptr, 0, sub.H, m, m, m, w, 1.0, s);
+    zgemm(false, G, w, Xn, w, nullptr, 0, sc.T2, m, w, m, w, 1.0, s, df);
+    zgemm(true, Xn, w, sc.T2, m, nullptr, 0, sub.H, m, m, m, w, 1.0, s, df);
     if ((e = bj_fp32(sub.H, m, sub, s, &sweeps)) != 0) return e;
-    if ((e = bj_refine(sub.H, m, sub, K1, refine_tol, s, &steps, &emax)) != 0) return e;
+    if ((e = bj_refine(sub.H, m, sub, K1, refine_tol, df, s, &steps, &emax)) != 0) return e;
     // X_N <- X_N U, the refined eigenvalues after those of the resolved part
-    zgemm(false, Xn, w, sub.X, m, nullptr, 0, sc.T2, m, w, m, m, 1.0, s);
+    zgemm(false, Xn, w, sub.X, m, nullptr, 0, sc.T2, m, w, m, m, 1.0, s, df);
     qm_note_launch();
     k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T2, m, Xn, w, w, m);
     ce = cudaMemcpyAsync(sc.lamK + r, sub.lamK, sizeof(double) * K1, cudaMemcpyDeviceToDevice, s);

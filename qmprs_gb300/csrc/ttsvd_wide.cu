@@ -51,8 +51,10 @@
 //    step), and the Gram of that subspace, X_N^H G X_N, whose scale is the
 //    small eigenvalues', is solved by the same two steps.
 // 3. k_bj_finalize: the refined eigenvalues in descending order, quimb's
-//    rsum2 cutoff from the trace (the tail sum is the trace minus the kept
-//    eigenvalues, so the unrefined columns never enter it); k_bj_emit, one
+//    rsum2 cutoff with the tail sums taken from the bottom (the refined
+//    small eigenvalues, plus the weight outside the refined columns from the
+//    trace of the deflated subproblem, so that no sum near the trace is
+//    subtracted from the trace); k_bj_emit, one
 //    block per kept column: canonical phase, the selected column and the
 //    site tensor of cut c.
 //
@@ -155,30 +157,31 @@ __global__ void k_bj_stats(const double* part, int nparts, const double2* G, int
 // Rotation of pair (p, q) of the 32 x 32 subproblem m: c, s e and s conj(e)
 // (the Rutishauser-style stable rotation that zeroes m[p][q]); flag 0 when
 // |m[p][q]| is below FP32 resolution (1e-7 relative, or floor_abs), big 1
-// when it is above 1e-5 relative (the sweep has not converged).
+// when it is above 1e-5 relative (the sweep has not converged).  Correctly
+// rounded reciprocal and square-root intrinsics.
 struct BJRot {
   float c;
-  float2 se, sce;
+  float2 se;
   int flag, big;
 };
 __device__ __forceinline__ BJRot bj_rot(const float2 (*m)[BJ_S + 1], int p, int q, float floor_abs, float big_abs) {
   BJRot r;
   const float2 g = m[p][q];
-  const float ag = sqrtf(g.x * g.x + g.y * g.y);
+  const float ag = __fsqrt_rn(g.x * g.x + g.y * g.y);
   const float app = m[p][p].x, aqq = m[q][q].x;
-  const float scale = sqrtf(fabsf(app * aqq));
+  const float scale = __fsqrt_rn(fabsf(app * aqq));
   r.flag = ag > floor_abs && ag > 1e-7f * scale;
   r.big = r.flag && ag > 1e-5f * scale && ag > big_abs;
   r.c = 1.f;
-  r.se = r.sce = cf(0.f, 0.f);
+  r.se = cf(0.f, 0.f);
   if (r.flag) {
-    const float zeta = (aqq - app) / (2.f * ag);
-    const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-    const float c = 1.f / sqrtf(1.f + t * t);
-    const float sg = c * t / ag;
+    const float inv = __frcp_rn(ag);
+    const float zeta = 0.5f * (aqq - app) * inv;
+    const float t = copysignf(__frcp_rn(fabsf(zeta) + __fsqrt_rn(fmaf(zeta, zeta, 1.f))), zeta);
+    const float c = __frsqrt_rn(fmaf(t, t, 1.f));
+    const float sg = c * t * inv;
     r.c = c;
     r.se = cf(g.x * sg, g.y * sg);
-    r.sce = cf(g.x * sg, -g.y * sg);
   }
   return r;
 }
@@ -186,13 +189,16 @@ __device__ __forceinline__ BJRot bj_rot(const float2 (*m)[BJ_S + 1], int p, int 
 // One block per pair of round k: one Jacobi sweep of the 32 x 32
 // subproblem; J (32 x 32, row-major) to Jbuf[pair]; the rotated diagonal
 // tile back into A.  count += 1 if a rotation was above 1e-5 relative.
-// Thread (gr, gc) owns the 2 x 2 entry group of inner pairs (gr, gc) and
-// computes both rotations itself; the subproblem is double-buffered (read
-// one copy, write the other), so an inner round takes one barrier.
+// Thread (gr, gc) owns the 2 x 2 entry group of inner pairs (gr, gc); lane
+// l of a warp computes the rotation of pair l % 16 (its gc) and takes gr's
+// from lane gr.  The subproblem is double-buffered (read one copy, write
+// the other), so an inner round takes one barrier; the inner rounds' pairs
+// come from a table built once.
 __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int nb, int k, float2* Jbuf,
                                                          const double* stats, int* count) {
   __shared__ float2 a[2][BJ_S][BJ_S + 1];
   __shared__ float2 j[BJ_S][BJ_S + 1];
+  __shared__ unsigned char tp[BJ_S - 1][BJ_S / 2], tq[BJ_S - 1][BJ_S / 2];
   __shared__ int s_big;
   const int pair = blockIdx.x, tid = threadIdx.x;
   if (tid == 0) s_big = 0;
@@ -201,6 +207,12 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
     a[0][r][c] = A[(int64_t)bj_index(nb, k, pair, r) * W + bj_index(nb, k, pair, c)];
     j[r][c] = cf(r == c ? 1.f : 0.f, 0.f);
   }
+  for (int e = tid; e < (BJ_S - 1) * (BJ_S / 2); e += blockDim.x) {
+    int p, q;
+    bj_pair(BJ_S, e / (BJ_S / 2), e % (BJ_S / 2), &p, &q);
+    tp[e / (BJ_S / 2)][e % (BJ_S / 2)] = (unsigned char)p;
+    tq[e / (BJ_S / 2)][e % (BJ_S / 2)] = (unsigned char)q;
+  }
   const float floor_abs = 1e-7f * (float)stats[0], big_abs = 1e-6f * (float)stats[0];
   __syncthreads();
   const int gr = tid / (BJ_S / 2), gc = tid % (BJ_S / 2);
@@ -208,16 +220,18 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
   for (int ir = 0; ir < BJ_S - 1; ++ir) {
     const float2 (*cur)[BJ_S + 1] = a[ir & 1];
     float2 (*nxt)[BJ_S + 1] = a[(ir + 1) & 1];
-    int pr, qr, pc, qc;
-    bj_pair(BJ_S, ir, gr, &pr, &qr);
-    bj_pair(BJ_S, ir, gc, &pc, &qc);
-    const BJRot rr = bj_rot(cur, pr, qr, floor_abs, big_abs);
-    const BJRot rcl = gr == gc ? rr : bj_rot(cur, pc, qc, floor_abs, big_abs);
+    const int pr = tp[ir][gr], qr = tq[ir][gr], pc = tp[ir][gc], qc = tq[ir][gc];
+    const BJRot rcl = bj_rot(cur, pc, qc, floor_abs, big_abs);
+    BJRot rr;
+    rr.c = __shfl_sync(0xffffffffu, rcl.c, gr);
+    rr.se.x = __shfl_sync(0xffffffffu, rcl.se.x, gr);
+    rr.se.y = __shfl_sync(0xffffffffu, rcl.se.y, gr);
+    rr.flag = __shfl_sync(0xffffffffu, rcl.flag, gr);
     big |= rcl.big;
     float2 x00 = cur[pr][pc], x01 = cur[pr][qc], x10 = cur[qr][pc], x11 = cur[qr][qc];
     if (rcl.flag) {   // columns: col_p <- c col_p - s conj(e) col_q ; col_q <- s e col_p + c col_q
       const float c = rcl.c;
-      const float2 se = rcl.se, sce = rcl.sce;
+      const float2 se = rcl.se, sce = cf(se.x, -se.y);
       const float2 n00 = cf(c * x00.x - (sce.x * x01.x - sce.y * x01.y), c * x00.y - (sce.x * x01.y + sce.y * x01.x));
       const float2 n01 = cf(se.x * x00.x - se.y * x00.y + c * x01.x, se.x * x00.y + se.y * x00.x + c * x01.y);
       const float2 n10 = cf(c * x10.x - (sce.x * x11.x - sce.y * x11.y), c * x10.y - (sce.x * x11.y + sce.y * x11.x));
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
     }
     if (rr.flag) {    // rows: row_p <- c row_p - s e row_q ; row_q <- s conj(e) row_p + c row_q
       const float c = rr.c;
-      const float2 se = rr.se, sce = rr.sce;
+      const float2 se = rr.se, sce = cf(se.x, -se.y);
       const float2 n00 = cf(c * x00.x - (se.x * x10.x - se.y * x10.y), c * x00.y - (se.x * x10.y + se.y * x10.x));
       const float2 n01 = cf(c * x01.x - (se.x * x11.x - se.y * x11.y), c * x01.y - (se.x * x11.y + se.y * x11.x));
       const float2 n10 = cf(sce.x * x00.x - sce.y * x00.y + c * x10.x, sce.x * x00.y + sce.y * x00.x + c * x10.y);
@@ -251,7 +265,8 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
     // J <- J R on the columns of pair gc, rows gr and gr + 16 (one owner each)
     if (rcl.flag) {
       const float c = rcl.c;
-      const float2 se = rcl.se, sce = rcl.sce;
+      const float2 se = rcl.se, sce = cf(se.x, -se.y);
+#pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int row = gr + h * (BJ_S / 2);
         const float2 vp = j[row][pc], vq = j[row][qc];
@@ -707,10 +722,20 @@ __global__ void k_bj_ns(double2* T, int m) {
 
 // Order of the refined eigenvalues and the rsum2 cutoff: bond c of state b
 // and order[] (the columns of X by descending eigenvalue).  The first Kr
-// columns of X are refined; at most K (<= Kr) are kept.  One block.
-__global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c, int w, int Kr, int K,
-                                                      const double* lamK, const double* stats, int* bonds,
-                                                      int max_bond, double cutoff, int* order, double* lsort) {
+// columns of X are refined; at most K (<= Kr) are kept.  The tail sums of
+// the rule are summed from the bottom: tail_from(i) = rest + sum_{i <= j <
+// Kr} l_j, where `rest` is the weight outside the refined columns: 0 when
+// all are refined; for a deflated cut (tr_sub non-null) the subproblem's
+// trace minus its refined eigenvalues (lamK[r .. Kr)), all at the small
+// eigenvalues' scale; otherwise trace - sum of the refined ones, which then
+// hold at most K <= r columns and leave resolved eigenvalues (above 1e-5 of
+// the largest, far above the cutoff) in the rest.  Subtracting ~1 - 1e-10
+// of the trace from the trace would carry the refined columns' rounding
+// into the decision.  One block.
+__global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c, int w, int Kr, int K, int r,
+                                                      const double* lamK, const double* stats, const double* tr_sub,
+                                                      int* bonds, int max_bond, double cutoff, int* order,
+                                                      double* lsort) {
   for (int i = threadIdx.x; i < Kr; i += blockDim.x) {
     const double li = lamK[i];
     int rank = 0;
@@ -724,25 +749,26 @@ __global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c,
   __syncthreads();
   int* bond = bonds + (int64_t)b * (bd.max_n + 1);
   if (threadIdx.x == 0) {
-    int keep;
-    if (K == w) {
-      keep = rank_by_cutoff(lsort, w, cutoff, max_bond);
-    } else {
-      // tail_from(i) = trace - sum_{j < i} l_j; keep = the largest i + 1
-      // with tail_from(i) > cutoff * trace, capped at K
-      const double total = stats[1];
-      double head = 0.0;
-      for (int i = 0; i < K; ++i) head += lsort[i] > 0.0 ? lsort[i] : 0.0;
-      keep = 0;
-      if (total - head > cutoff * total) keep = K;
-      for (int i = K - 1; i >= 0 && keep == 0; --i) {
-        head -= lsort[i] > 0.0 ? lsort[i] : 0.0;
-        if (total - head > cutoff * total) keep = i + 1;
-      }
-      if (keep < 1) keep = 1;
-      if (max_bond > 0 && keep > max_bond) keep = max_bond;
+    const double total = stats[1];
+    double rest = 0.0;
+    if (tr_sub) {
+      rest = *tr_sub;
+      for (int i = r; i < Kr; ++i) rest -= lamK[i];
+    } else if (Kr < w) {
+      rest = total;
+      for (int i = 0; i < Kr; ++i) rest -= lamK[i];
     }
-    if (keep > K) keep = K;
+    if (rest < 0.0) rest = 0.0;
+    double tail = rest;
+    for (int i = Kr - 1; i >= K; --i) tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
+    int keep = 0;
+    if (tail > cutoff * total) keep = K;   // tail_from(K): more than K would be kept
+    for (int i = K - 1; i >= 0 && keep == 0; --i) {
+      tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
+      if (tail > cutoff * total) keep = i + 1;
+    }
+    if (keep < 1) keep = 1;
+    if (max_bond > 0 && keep > max_bond) keep = max_bond;
     if (keep > bd.tt_b) keep = bd.tt_b;
     if (c < 30 && keep > (1 << c)) keep = 1 << c;
     bond[c] = keep;
@@ -1050,7 +1076,8 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, B
   while (Kr < w && Kr < sc.kmax && Kr < K + BJ_EXTRA && lam[Kr] >= lam[K - 1] - BJ_MARGIN * lam[0]) ++Kr;
   int r = 0;
   while (r < w && lam[r] > BJ_RESOLVED * lam[0]) ++r;
-  if (Kr <= r || r == 0) {
+  const bool deflated = !(Kr <= r || r == 0);
+  if (!deflated) {
     e = bj_refine(G, w, sc, Kr, refine_tol, df, s, &steps, &emax);
     if (e) return e;
   } else {
@@ -1079,8 +1106,8 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, B
     if (ce != cudaSuccess) return (int)ce;
   }
   qm_note_launch();
-  k_bj_finalize<<<1, 1024, 0, s>>>(bd, b, c, w, Kr, K, sc.lamK, sc.stats, bonds, max_bond, cutoff, sc.order,
-                                    sc.lsort);
+  k_bj_finalize<<<1, 1024, 0, s>>>(bd, b, c, w, Kr, K, r, sc.lamK, sc.stats, deflated ? sub.stats + 1 : nullptr,
+                                    bonds, max_bond, cutoff, sc.order, sc.lsort);
   qm_note_launch();
   k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.X, w, bonds, sc.order, vsel, bd.tt_b, tensors, chi);
   if (st) {

@@ -433,8 +433,8 @@ int exact_mps_from_statevector(qmprs_plan* p, const double2* sv, int max_bond, d
         if (c < 1) continue;
         const int r = hb[(size_t)b * stride + c + 1];
         if (r < 1 || r > p->tt_b || 2 * r <= p->bd.eig_wmax) continue;
-        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, p->bj, p->bj_sub, bonds, p->vsel2, tensors, p->max_bond,
-                                   max_bond, cutoff, BJ_TOL_EXACT, s, &p->bj_stats);
+        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, nullptr, p->bj, p->bj_sub, bonds, p->vsel2, tensors,
+                                   p->max_bond, max_bond, cutoff, BJ_TOL_EXACT, s, &p->bj_stats);
         if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) blocked eigensolver");
       }
     }
@@ -940,8 +940,10 @@ int qmprs_mps_from_statevector(qmprs_plan_t p, const void* sv_, int max_bond, do
         if (c < 1) continue;
         const int r = hb[(size_t)b * stride + c + 1];
         if (r < 1 || r > p->tt_b || 2 * r <= p->bd.eig_wmax) continue;
-        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, p->bj, p->bj_sub, bonds, p->vsel2, tensors, p->max_bond,
-                                   max_bond, cutoff, BJ_TOL_FAST, s, &p->bj_stats);
+        // fewer remainder rows than Gram columns: the row Gram (rank <= 2^c)
+        const float2* rowsrc = ipow2(c) < 2 * r ? src + p->vec_off[b] : nullptr;
+        const int e = tt_block_eig(p->bd, b, c, 2 * r, p->gram, rowsrc, p->bj, p->bj_sub, bonds, p->vsel2, tensors,
+                                   p->max_bond, max_bond, cutoff, BJ_TOL_FAST, s, &p->bj_stats);
         if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "stage (a) blocked eigensolver");
         any = true;
       }

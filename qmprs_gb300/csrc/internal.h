@@ -196,12 +196,13 @@ void launch_tt_site0(const BatchDev& bd, const float2* rem0, const float2* rem1,
 // Scratch of the blocked eigensolver for Grams wider than TT_MAXW (one
 // state at a time): FP32 matrix and eigenvectors (W x W, W = width rounded
 // up to 32), the subproblem rotations, the FP64 basis X, the input of a
-// deflated subproblem H, two FP64 work matrices, and the refinement
+// deflated subproblem H, two FP64 work matrices, the conjugate transpose
+// of a remainder for the row-Gram path, and the refinement
 // products [H X_K | X_K] and [S | X^H X_K] (n x 2K).
 struct BJScratch {
   int W = 0, kmax = 0;
   float2 *A = nullptr, *V = nullptr, *J = nullptr;
-  double2 *X = nullptr, *H = nullptr, *T = nullptr, *T2 = nullptr, *YX = nullptr, *SR = nullptr;
+  double2 *X = nullptr, *H = nullptr, *T = nullptr, *T2 = nullptr, *Mt = nullptr, *YX = nullptr, *SR = nullptr;
   int *perm = nullptr, *order = nullptr, *count = nullptr;
   double *lamA = nullptr, *lamK = nullptr, *lsort = nullptr, *stats = nullptr, *part = nullptr;
   unsigned* emax = nullptr;
@@ -220,9 +221,13 @@ struct BJStats {
 };
 int bj_alloc(BJScratch& sc, int tt_w, int tt_b);
 void bj_free(BJScratch& sc);
-int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, BJScratch& sc, BJScratch& sub,
-                 int* bonds, double2* vsel, double2* tensors, int chi, int max_bond, double cutoff, double refine_tol,
-                 cudaStream_t s, BJStats* st);
+// Diagonalise stage (a)'s Gram of state b at cut c and emit the cut: the
+// w x w column Gram already in `gram`, or, with rowsrc (the 2^c x w
+// complex64 remainder, 2^c < w), the row Gram M M^H built here, whose kept
+// right singular vectors are M^H U Sigma^-1.
+int tt_block_eig(const BatchDev& bd, int b, int c, int w, double2* gram, const float2* rowsrc,
+                 BJScratch& sc, BJScratch& sub, int* bonds, double2* vsel, double2* tensors, int chi, int max_bond,
+                 double cutoff, double refine_tol, cudaStream_t s, BJStats* st);
 void launch_cgemm(const float2* A, int64_t lda, const double2* B, int64_t ldb, float2* C, int64_t ldc, int64_t M,
                   int N, int K, cudaStream_t s);
 void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,

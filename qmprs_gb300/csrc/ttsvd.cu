@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_tt_gram(BatchDev bd, int step
       continue;
     }
     const int w = 2 * r;
+    if (w > bd.eig_wmax && ipow2(c) < (int64_t)w) continue;   // the row Gram (ttsvd_wide.cu)
     const int nt = bd.state_ntiles[b];
     const int nsplit = nt < TT_SPLIT ? nt : TT_SPLIT;
     const float2* m = (step == 0 ? sv : src) + bd.vec_off[b];

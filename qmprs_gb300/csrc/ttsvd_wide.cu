@@ -775,12 +775,13 @@ __global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c,
   }
 }
 
-// One block per kept column l (order[l] of X): the canonical phase (the
-// pivot rule of phase_fix_column: the lowest row whose magnitude is within
-// QM_PIVOT_TOL of the column's largest, made real positive), the selected
-// column into vsel (stride vstride) and row l of the site tensor of cut c.
-__global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, int c, const double2* X, int w,
-                                                           const int* bonds, const int* order, double2* vsel,
+// One block per kept column l (column order[l] of X, or column l without
+// order; w entries, row stride ldx): the canonical phase (the pivot rule of
+// phase_fix_column: the lowest row whose magnitude is within QM_PIVOT_TOL of
+// the column's largest, made real positive), the selected column into vsel
+// (stride vstride) and row l of the site tensor of cut c.
+__global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, int c, const double2* X, int ldx,
+                                                           int w, const int* bonds, const int* order, double2* vsel,
                                                            int vstride, double2* tensors, int chi) {
   __shared__ double s_m[BLOCK_THREADS / 32];
   __shared__ int s_j[BLOCK_THREADS / 32];
@@ -788,10 +789,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, i
   const int l = blockIdx.x;
   const int keep = bonds[(int64_t)b * (bd.max_n + 1) + c];
   if (l >= keep) return;
-  const int col = order[l];
+  const int col = order ? order[l] : l;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double m = -1.0;
-  for (int i = threadIdx.x; i < w; i += blockDim.x) m = fmax(m, cabs_(X[(int64_t)i * w + col]));
+  for (int i = threadIdx.x; i < w; i += blockDim.x) m = fmax(m, cabs_(X[(int64_t)i * ldx + col]));
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) s_m[warp] = m;
   __syncthreads();
@@ -799,7 +800,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, i
   for (int k = 1; k < BLOCK_THREADS / 32; ++k) m = fmax(m, s_m[k]);
   int jp = w;
   for (int i = threadIdx.x; i < w; i += blockDim.x)
-    if (cabs_(X[(int64_t)i * w + col]) >= (1.0 - QM_PIVOT_TOL) * m) {
+    if (cabs_(X[(int64_t)i * ldx + col]) >= (1.0 - QM_PIVOT_TOL) * m) {
       jp = i;
       break;
     }
@@ -810,7 +811,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, i
     int j = s_j[0];
     for (int k = 1; k < BLOCK_THREADS / 32; ++k) j = min(j, s_j[k]);
     if (j >= w) j = 0;
-    const double2 z = X[(int64_t)j * w + col];
+    const double2 z = X[(int64_t)j * ldx + col];
     const double az = cabs_(z);
     s_ph = az > 0.0 ? cscale(cconj(z), 1.0 / az) : cd(1.0, 0.0);
   }
@@ -821,9 +822,37 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_emit(BatchDev bd, int b, i
   const int ce = chi < (1 << (n / 2)) ? chi : (1 << (n / 2));
   double2* ts = tensors + bd.tensor_off[b] + (int64_t)c * 2 * ce * ce + (int64_t)l * w;
   for (int i = threadIdx.x; i < w; i += blockDim.x) {
-    const double2 v = cmul(X[(int64_t)i * w + col], ph);
+    const double2 v = cmul(X[(int64_t)i * ldx + col], ph);
     vs[(int64_t)i * vstride + l] = v;
     ts[i] = cconj(v);
+  }
+}
+
+// Row-Gram path.  Mt = M^H (w x rows, FP64) of the complex64 remainder M
+// (rows x w): 32 x 32 tiles transposed through shared memory.
+__global__ void k_bj_mt(const float2* M, int rows, int w, double2* Mt) {
+  __shared__ float2 t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    const int rr = e / 32, cc = e % 32;
+    t[rr][cc] = (r0 + rr < rows && c0 + cc < w) ? M[(int64_t)(r0 + rr) * w + c0 + cc] : cf(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+    const int cc = e / 32, rr = e % 32;
+    if (c0 + cc < w && r0 + rr < rows) Mt[(int64_t)(c0 + cc) * rows + r0 + rr] = cd(t[rr][cc].x, -t[rr][cc].y);
+  }
+}
+
+// U (n x K, row stride K): column l = X[:, order[l]] / sigma_l, sigma_l the
+// square root of the l-th eigenvalue (descending); then V = M^H U holds the
+// right singular vectors of the kept values.
+__global__ void k_bj_gather(const double2* X, int n, const int* order, const double* lsort, int K, double2* U) {
+  const int64_t total = (int64_t)n * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / K), l = (int)(e % K);
+    const double lam = lsort[l];
+    U[e] = lam > 0.0 ? cscale(X[(int64_t)i * n + order[l]], 1.0 / sqrt(lam)) : czero();
   }
 }
 
@@ -908,6 +937,7 @@ int bj_alloc(BJScratch& sc, int tt_w, int tt_b) {
   get(reinterpret_cast<void**>(&sc.H), sizeof(double2) * WW);
   get(reinterpret_cast<void**>(&sc.T), sizeof(double2) * WW);
   get(reinterpret_cast<void**>(&sc.T2), sizeof(double2) * WW);
+  get(reinterpret_cast<void**>(&sc.Mt), sizeof(double2) * WW);
   get(reinterpret_cast<void**>(&sc.YX), sizeof(double2) * (size_t)W * 2 * kmax);
   get(reinterpret_cast<void**>(&sc.SR), sizeof(double2) * (size_t)W * 2 * kmax);
   get(reinterpret_cast<void**>(&sc.perm), sizeof(int) * W);
@@ -923,7 +953,7 @@ int bj_alloc(BJScratch& sc, int tt_w, int tt_b) {
 }
 
 void bj_free(BJScratch& sc) {
-  void* ptrs[] = {sc.A,     sc.V,     sc.J,     sc.X,    sc.H,     sc.T,     sc.T2,   sc.YX,  sc.SR,
+  void* ptrs[] = {sc.A,     sc.V,     sc.J,     sc.X,    sc.H,     sc.T,     sc.T2,   sc.Mt,  sc.YX,  sc.SR,
                   sc.perm,  sc.order, sc.count, sc.lamA, sc.lamK, sc.lsort, sc.stats, sc.part, sc.emax};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -1049,13 +1079,22 @@ static int bj_refine(const double2* H, int n, BJScratch& sc, int Kc, double tol,
 // X_N^H G X_N, whose scale is that of the small eigenvalues, is solved the
 // same way in `sub`.  Synchronises the stream once per sweep and per
 // refinement step.  Returns a cudaError_t.
-int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, BJScratch& sc, BJScratch& sub,
-                 int* bonds, double2* vsel, double2* tensors, int chi, int max_bond, double cutoff, double refine_tol,
-                 cudaStream_t s, BJStats* st) {
-  const double2* G = gram + (int64_t)b * bd.tt_w * bd.tt_w;
+int tt_block_eig(const BatchDev& bd, int b, int c, int wv, double2* gram, const float2* rowsrc,
+                 BJScratch& sc, BJScratch& sub, int* bonds, double2* vsel, double2* tensors, int chi, int max_bond,
+                 double cutoff, double refine_tol, cudaStream_t s, BJStats* st) {
+  double2* G = gram + (int64_t)b * bd.tt_w * bd.tt_w;
   // the fast mode's tolerance leaves about 1e-8 of error: double-float
   // refinement products suffice there; the exact mode takes FP64 products
   const bool df = refine_tol > BJ_TOL_EXACT;
+  // the Gram's size: the column Gram (wv), or the row Gram M M^H of the
+  // 2^c x wv remainder
+  const int w = rowsrc ? (int)ipow2(c) : wv;
+  if (rowsrc) {
+    if (w > sc.W || wv > sc.W) return (int)cudaErrorInvalidValue;
+    qm_note_launch();
+    k_bj_mt<<<dim3((wv + 31) / 32, (w + 31) / 32), BLOCK_THREADS, 0, s>>>(rowsrc, w, wv, sc.Mt);
+    zgemm(true, sc.Mt, w, sc.Mt, w, nullptr, 0, G, w, w, w, wv, 1.0, s, true);
+  }
   int sweeps = 0, steps = 0;
   float emax = 0.f;
   int e = bj_fp32(G, w, sc, s, &sweeps);
@@ -1108,8 +1147,16 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int w, const double2* gram, B
   qm_note_launch();
   k_bj_finalize<<<1, 1024, 0, s>>>(bd, b, c, w, Kr, K, r, sc.lamK, sc.stats, deflated ? sub.stats + 1 : nullptr,
                                     bonds, max_bond, cutoff, sc.order, sc.lsort);
-  qm_note_launch();
-  k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.X, w, bonds, sc.order, vsel, bd.tt_b, tensors, chi);
+  if (rowsrc) {   // V = M^H U Sigma^-1 (wv x K), then emitted in order
+    qm_note_launch();
+    k_bj_gather<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.X, w, sc.order, sc.lsort, K, sc.T);
+    zgemm(false, sc.Mt, w, sc.T, K, nullptr, 0, sc.T2, K, wv, K, w, 1.0, s, true);
+    qm_note_launch();
+    k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.T2, K, wv, bonds, nullptr, vsel, bd.tt_b, tensors, chi);
+  } else {
+    qm_note_launch();
+    k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.X, w, w, bonds, sc.order, vsel, bd.tt_b, tensors, chi);
+  }
   if (st) {
     st->sweeps += sweeps;
     st->refine_steps += steps;

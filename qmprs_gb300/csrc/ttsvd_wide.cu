@@ -16,7 +16,8 @@
 //                   the round (upper triangle, mirrored) and V[:,Q] <- V J_Q.
 //    Sweeps run until one sweep makes no rotation larger than 1e-5 of
 //    sqrt(a_pp a_qq) (at most BJ_MAX_SWEEPS); rotations below FP32
-//    resolution (1e-7 relative, or 1e-7 of ||G||_F absolute) are skipped.
+//    resolution (1e-7 relative, or 1e-7 of ||G||_F / sqrt(W) absolute) are
+//    skipped.
 // 2. FP64 refinement of the K columns that can be kept (K = min(w,
 //    max_bond, bond capacity, 2^c)), and of the discarded ones whose FP32
 //    eigenvalue lies within 1e-5 (of the largest) of the last kept one
@@ -81,6 +82,7 @@
 #define BJ_NOISE 1e-6       // eigenvalues below this fraction of the largest are FP32 noise
 #define BJ_MARGIN 1e-5      // discarded columns this close (of the largest) to the last kept one ...
 #define BJ_EXTRA 32         // ... are refined too, at most this many
+#define BJ_ONE_SIDED 0.3    // largest rotation against an unrefined column
 
 // Pair i of round k of the round-robin tournament over n (even) indices.
 __host__ __device__ inline void bj_pair(int n, int k, int i, int* p, int* q) {
@@ -213,7 +215,11 @@ __global__ void __launch_bounds__(BJ_THREADS) k_bj_solve(float2* A, int W, int n
     tp[e / (BJ_S / 2)][e % (BJ_S / 2)] = (unsigned char)p;
     tq[e / (BJ_S / 2)][e % (BJ_S / 2)] = (unsigned char)q;
   }
-  const float floor_abs = 1e-7f * (float)stats[0], big_abs = 1e-6f * (float)stats[0];
+  // rotations below FP32 rounding of the entries are skipped: ||G||_F /
+  // sqrt(W) is the entries' scale (||G||_F alone overstates it by up to
+  // sqrt(W) on flat spectra, where a floor that high leaves couplings at a
+  // third of the eigenvalue gaps)
+  const float floor_abs = 1e-7f * (float)stats[0] * rsqrtf((float)W), big_abs = 1e-6f * (float)stats[0];
   __syncthreads();
   const int gr = tid / (BJ_S / 2), gc = tid % (BJ_S / 2);
   int big = 0;
@@ -675,9 +681,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_correct(double2* SR, int n
       const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       const double c = 1.0 / sqrt(1.0 + t * t);
       const double sn = c * t;
-      ev = cscale(num, sn / an);
-      dsum -= t * t * c * c / (1.0 + c);   // c - 1
-      mx = fmaxf(mx, (float)fabs(sn));
+      if (i >= Kc && fabs(sn) > BJ_ONE_SIDED) {
+        // against an unrefined column only one side moves: a rotation this
+        // large would mix the pair without converging; the caller keeps
+        // near-degenerate partners refined on both sides
+        ev = czero();
+      } else {
+        ev = cscale(num, sn / an);
+        dsum -= t * t * c * c / (1.0 + c);   // c - 1
+        mx = fmaxf(mx, (float)fabs(sn));
+      }
     }
     SR[o + jc] = ev;
   }
@@ -842,6 +855,12 @@ __global__ void k_bj_mt(const float2* M, int rows, int w, double2* Mt) {
     const int cc = e / 32, rr = e % 32;
     if (c0 + cc < w && r0 + rr < rows) Mt[(int64_t)(c0 + cc) * rows + r0 + rr] = cd(t[rr][cc].x, -t[rr][cc].y);
   }
+}
+
+// dst = src in FP64 (count complex entries).
+__global__ void k_bj_f2d(const float2* src, int64_t count, double2* dst) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = f2d(src[e]);
 }
 
 // U (n x K, row stride K): column l = X[:, order[l]] / sigma_l, sigma_l the
@@ -1088,7 +1107,7 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int wv, double2* gram, const 
   const bool df = refine_tol > BJ_TOL_EXACT;
   // the Gram's size: the column Gram (wv), or the row Gram M M^H of the
   // 2^c x wv remainder
-  const int w = rowsrc ? (int)ipow2(c) : wv;
+  int w = rowsrc ? (int)ipow2(c) : wv;
   if (rowsrc) {
     if (w > sc.W || wv > sc.W) return (int)cudaErrorInvalidValue;
     qm_note_launch();
@@ -1097,24 +1116,45 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int wv, double2* gram, const 
   }
   int sweeps = 0, steps = 0;
   float emax = 0.f;
-  int e = bj_fp32(G, w, sc, s, &sweeps);
-  if (e) return e;
-  int K = w;
-  if (max_bond > 0 && K > max_bond) K = max_bond;
-  if (K > bd.tt_b) K = bd.tt_b;
-  if (c < 30 && K > (1 << c)) K = 1 << c;
-  if (K > sc.kmax) return (int)cudaErrorInvalidValue;
-  std::vector<double> lam(w);
-  cudaError_t ce = cudaMemcpyAsync(lam.data(), sc.lamA, sizeof(double) * w, cudaMemcpyDeviceToHost, s);
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-  if (ce != cudaSuccess) return (int)ce;
-  // refined columns: the K that may be kept and the discarded ones whose
-  // FP32 eigenvalue is within BJ_MARGIN of the last kept one (their order
-  // and their mixing with it are below FP32 resolution)
-  int Kr = K;
-  while (Kr < w && Kr < sc.kmax && Kr < K + BJ_EXTRA && lam[Kr] >= lam[K - 1] - BJ_MARGIN * lam[0]) ++Kr;
-  int r = 0;
-  while (r < w && lam[r] > BJ_RESOLVED * lam[0]) ++r;
+  int e = 0, K = 0, Kr = 0, r = 0;
+  std::vector<double> lam;
+  cudaError_t ce = cudaSuccess;
+  for (;;) {
+    if ((e = bj_fp32(G, w, sc, s, &sweeps)) != 0) return e;
+    K = w;
+    if (max_bond > 0 && K > max_bond) K = max_bond;
+    if (K > bd.tt_b) K = bd.tt_b;
+    if (c < 30 && K > (1 << c)) K = 1 << c;
+    if (K > sc.kmax) return (int)cudaErrorInvalidValue;
+    lam.resize(w);
+    ce = cudaMemcpyAsync(lam.data(), sc.lamA, sizeof(double) * w, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return (int)ce;
+    // refined columns: the K that may be kept and the discarded ones whose
+    // FP32 eigenvalue is within BJ_MARGIN of the last kept one (their order
+    // and their mixing with it are below FP32 resolution)
+    Kr = K;
+    while (Kr < w && Kr < sc.kmax && Kr < K + BJ_EXTRA && lam[Kr] >= lam[K - 1] - BJ_MARGIN * lam[0]) ++Kr;
+    r = 0;
+    while (r < w && lam[r] > BJ_RESOLVED * lam[0]) ++r;
+    // the split between refined and deflated columns sits at a gap (5% of
+    // the eigenvalue, and 1e-6 of the largest): the pairs across it are
+    // refined from one side only, which cannot resolve near-degenerate ones
+    while (r > 0 && r < w && lam[r - 1] - lam[r] < fmax(0.05 * lam[r - 1], 1e-6 * lam[0])) --r;
+    // the row Gram's kept right vectors M^H u / sigma carry the eigenvector
+    // error times sigma_1 / sigma: kept only while every refined column is
+    // resolved (sigma_1 / sigma < 316); otherwise the column Gram of the
+    // same remainder, M^H M, in double-float products
+    if (rowsrc && Kr > r) {
+      qm_note_launch();
+      k_bj_f2d<<<BJ_EB, BLOCK_THREADS, 0, s>>>(rowsrc, (int64_t)w * wv, sc.T);
+      zgemm(true, sc.T, wv, sc.T, wv, nullptr, 0, G, wv, wv, wv, w, 1.0, s, true);
+      rowsrc = nullptr;
+      w = wv;
+      continue;
+    }
+    break;
+  }
   const bool deflated = !(Kr <= r || r == 0);
   if (!deflated) {
     e = bj_refine(G, w, sc, Kr, refine_tol, df, s, &steps, &emax);
@@ -1151,6 +1191,18 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int wv, double2* gram, const 
     qm_note_launch();
     k_bj_gather<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.X, w, sc.order, sc.lsort, K, sc.T);
     zgemm(false, sc.Mt, w, sc.T, K, nullptr, 0, sc.T2, K, wv, K, w, 1.0, s, true);
+    // the division by sigma_l amplifies the eigenvector's error by
+    // sigma_1 / sigma_l: two Newton-Schulz steps V <- V (3I - V^H V) / 2
+    // restore the isometry (the kept subspace keeps an error of at most
+    // that amplification, weighted by sigma_l in the truncated state)
+    for (int ns = 0; ns < 2; ++ns) {
+      zgemm(true, sc.T2, K, sc.T2, K, nullptr, 0, sc.H, K, K, K, wv, 1.0, s, true);
+      qm_note_launch();
+      k_bj_ns<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.H, K);
+      zgemm(false, sc.T2, K, sc.H, K, nullptr, 0, sc.T, K, wv, K, K, 1.0, s, true);
+      qm_note_launch();
+      k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T, K, sc.T2, K, wv, K);
+    }
     qm_note_launch();
     k_bj_emit<<<K, BLOCK_THREADS, 0, s>>>(bd, b, c, sc.T2, K, wv, bonds, nullptr, vsel, bd.tt_b, tensors, chi);
   } else {

@@ -29,8 +29,8 @@
 //      E_ij = s_ij e_ij,  E_jj = R_jj / 2 + sum_i (c_ij - 1),
 //    where (c_ij, s_ij e_ij) is the rotation that diagonalises the 2 x 2
 //    block [[l_j, conj(b)], [b, l_i]], b = S_ij + l_j R_ij (to first order
-//    E_ij = b / (l_j - l_i), the published step; the full rotation also
-//    resolves near-degenerate pairs), and
+//    E_ij = b / (l_j - l_i), the published step; the full rotation is
+//    taken up to |s| = 0.3, beyond which a pair counts as a cluster), and
 //      X_K <- X_K + X E.
 //    S and R are FP64 products (k_zgemm) in the exact mode and double-float
 //    products on the FP32 pipes (k_zgemm_df, about 5x the FP64 rate) in the
@@ -82,7 +82,7 @@
 #define BJ_NOISE 1e-6       // eigenvalues below this fraction of the largest are FP32 noise
 #define BJ_MARGIN 1e-5      // discarded columns this close (of the largest) to the last kept one ...
 #define BJ_EXTRA 32         // ... are refined too, at most this many
-#define BJ_ONE_SIDED 0.3    // largest rotation against an unrefined column
+#define BJ_MAX_ROT 0.3       // largest rotation (sin) a refinement step takes per pair
 
 // Pair i of round k of the round-robin tournament over n (even) indices.
 __host__ __device__ inline void bj_pair(int n, int k, int i, int* p, int* q) {
@@ -681,11 +681,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_bj_correct(double2* SR, int n
       const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       const double c = 1.0 / sqrt(1.0 + t * t);
       const double sn = c * t;
-      if (i >= Kc && fabs(sn) > BJ_ONE_SIDED) {
-        // against an unrefined column only one side moves: a rotation this
-        // large would mix the pair without converging; the caller keeps
-        // near-degenerate partners refined on both sides
-        ev = czero();
+      if (fabs(sn) > BJ_MAX_ROT) {
+        // a near-degenerate pair (at the FP32 sweeps' resolution): rotations
+        // this large over overlapping pairs of a dense cluster do not add up
+        // to a unitary and diverge; the pair keeps its FP32 mixing (between
+        // two refined columns only the orthonormality is restored; against
+        // an unrefined column nothing moves)
+        ev = i < Kc ? cscale(rv, 0.5) : czero();
       } else {
         ev = cscale(num, sn / an);
         dsum -= t * t * c * c / (1.0 + c);   // c - 1
@@ -1165,13 +1167,21 @@ int tt_block_eig(const BatchDev& bd, int b, int c, int wv, double2* gram, const 
     if (e) return e;
     if (sub.W == 0 && (e = bj_alloc(sub, sc.W, sc.kmax)) != 0) return e;
     double2* Xn = sc.X + r;   // row stride w
-    // X_N <- X_N - X_R (X_R^H X_N), then one Newton-Schulz step
+    // X_N <- X_N - X_R (X_R^H X_N), then Newton-Schulz steps (the refined
+    // columns took small one-sided corrections towards X_N, so the
+    // projection shortens some columns by up to a few percent)
     zgemm(true, sc.X, w, Xn, w, nullptr, 0, sc.T, m, r, m, w, 1.0, s, df);
     zgemm(false, sc.X, w, sc.T, m, Xn, w, sc.T2, m, w, m, r, -1.0, s, df);
-    zgemm(true, sc.T2, m, sc.T2, m, nullptr, 0, sc.T, m, m, m, w, 1.0, s, df);
-    qm_note_launch();
-    k_bj_ns<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T, m);
-    zgemm(false, sc.T2, m, sc.T, m, nullptr, 0, Xn, w, w, m, m, 1.0, s, df);
+    for (int ns = 0; ns < 4; ++ns) {
+      zgemm(true, sc.T2, m, sc.T2, m, nullptr, 0, sc.T, m, m, m, w, 1.0, s, df);
+      qm_note_launch();
+      k_bj_ns<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.T, m);
+      zgemm(false, sc.T2, m, sc.T, m, nullptr, 0, ns == 3 ? Xn : sc.YX, ns == 3 ? w : m, w, m, m, 1.0, s, df);
+      if (ns < 3) {
+        qm_note_launch();
+        k_bj_copy<<<BJ_EB, BLOCK_THREADS, 0, s>>>(sc.YX, m, sc.T2, m, w, m);
+      }
+    }
     // Gram of the unresolved subspace, solved in `sub`
     zgemm(false, G, w, Xn, w, nullptr, 0, sc.T2, m, w, m, w, 1.0, s, df);
     zgemm(true, Xn, w, sc.T2, m, nullptr, 0, sub.H, m, m, m, w, 1.0, s, df);

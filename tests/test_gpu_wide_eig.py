@@ -78,3 +78,29 @@ def test_wide_exact_mode_tolerance(eng):
     ts = D.tt_svd_right(sv / np.linalg.norm(sv), n, chi)
     got = target.cpu().numpy().view(np.complex128)
     assert np.max(np.abs(got - D.mps_to_dense(ts))) < 1e-9
+
+
+@pytest.mark.parametrize("seed", [3, 11])
+def test_wide_decaying_spectra_keep_isometric_tensors(eng, seed):
+    """Gaussian-mixture states with random phases (20 qubits, bond 256):
+    decaying spectra send cuts through the deflated subproblem and the row
+    Gram.  Every site tensor stays right-isometric (A A^H = I) and the
+    truncated target keeps the input's norm, as the rsum2 renormalisation
+    does."""
+    import torch
+    n, chi = 20, 256
+    sv = S.gaussian_mixture(n, seed)
+    p, svd = eng.upload([sv], 1, chi)
+    tensors, bonds, target = eng.stage_mps(p, svd, chi)
+    tn = eng.overlap(p, target, target).cpu().numpy()[0]
+    assert abs(tn - 1.0) < 1e-6, tn
+    torch.cuda.synchronize()
+    bd = [int(x) for x in bonds.cpu().numpy()[: n + 1]]
+    ce = min(chi, 2 ** (n // 2))
+    t = tensors.cpu().numpy().view(np.complex128)
+    base = int(p.tensor_off[0])
+    for c in range(1, n):
+        keep, w = bd[c], 2 * bd[c + 1]
+        a = t[base + c * 2 * ce * ce: base + c * 2 * ce * ce + keep * w].reshape(keep, w)
+        err = np.max(np.abs(a @ a.conj().T - np.eye(keep)))
+        assert err < 1e-5, (c, keep, w, err)

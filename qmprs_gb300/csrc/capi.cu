@@ -521,6 +521,12 @@ int exact_optimize_layers(qmprs_plan* p, const double2* target, double2* gates, 
   launch_fill_int(p->active, p->B, 1, s);
   launch_x_from_d(p->bd, target, p->XT, s);
   launch_x_dot(p->bd, p->XT, p->XT, p->partials, p->tnorm, s);
+  if (p->max_n <= X_FUSED_MAXN) {   // every state fits one block's shared memory
+    const int e = launch_x_sweep_fused(p->bd, p->max_n, p->XT, gates, ar, num_layers, p->active, p->tnorm,
+                                       num_sweeps, stop_fidelity, sweep_fid, sweeps_done, s);
+    if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "k_x_sweep_fused");
+    return check_kernel_errors(p, s);
+  }
   xc* psi = p->X0;
   xc* t = p->X1;
   auto body = [&](cudaStream_t s2, bool capturing) -> int {

@@ -668,6 +668,195 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_x_sweep_step(BatchDev bd, int
   }
 }
 
+// Every sweep of a state in one block (states of at most X_FUSED_MAXN
+// qubits): psi and t as double-float in shared memory, the same steps as
+// the launch-per-step path (k_x_apply_gate / k_x_sweep_step /
+// k_sweep_finish): C|0> rebuilt gate by gate, t from the target, then per
+// gate (backward order) psi <- G^H psi, E = sum conj(t) psi, the FP64
+// polar factor by thread 0 (G <- conj(W)), t <- G^H t; after the sweep
+// the fidelity nuc / ||target||, the sweep count and the stop at
+// stop_fidelity.  The environment is reduced per warp (fixed butterfly)
+// and over the warps in order.
+__device__ __forceinline__ void x_fused_apply(xc* v, int n, int q, int k, const xc* gs) {
+  if (k == 2) {
+    const int slo = n - 2 - q;
+    const int64_t dlo = (int64_t)1 << slo, dhi = dlo << 1;
+    for (int64_t r = threadIdx.x; r < ipow2(n - 2); r += blockDim.x) {
+      const int64_t i0 = quad_base(r, slo);
+      const int64_t idx[4] = {i0, i0 + dlo, i0 + dhi, i0 + dhi + dlo};
+      xc x[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) x[a] = v[idx[a]];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        XA acc = xa_zero();
+#pragma unroll
+        for (int c = 0; c < 4; ++c) xa_mac(acc, gs[a * 4 + c], x[c]);
+        v[idx[a]] = xa_round(acc);
+      }
+    }
+  } else {
+    const int bit = n - 1 - q;
+    const int64_t d = (int64_t)1 << bit;
+    for (int64_t r = threadIdx.x; r < ipow2(n - 1); r += blockDim.x) {
+      const int64_t i0 = pair_base(r, bit);
+      const xc x0 = v[i0], x1 = v[i0 + d];
+      XA s0 = xa_zero(), s1 = xa_zero();
+      xa_mac(s0, gs[0], x0);
+      xa_mac(s0, gs[1], x1);
+      xa_mac(s1, gs[2], x0);
+      xa_mac(s1, gs[3], x1);
+      v[i0] = xa_round(s0);
+      v[i0 + d] = xa_round(s1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BLOCK_THREADS) k_x_sweep_fused(BatchDev bd, const xc* target, double2* gates,
+                                                                 const signed char* arity, const int* nlayers,
+                                                                 int* active, const double2* tnorm2, int num_sweeps,
+                                                                 double stop_fid, double* sweep_fid,
+                                                                 int* sweeps_done) {
+  extern __shared__ xc xsm[];
+  __shared__ xc gs[16];
+  __shared__ double2 wred[WARPS][16];
+  __shared__ double2 env[16];
+  __shared__ double s_nuc;
+  const int b = blockIdx.x;
+  if (b >= bd.B) return;
+  const int n = bd.n[b];
+  const int64_t N = ipow2(n);
+  xc* psi = xsm;
+  xc* tt = xsm + N;
+  const int L = nlayers[b];
+  const int G = L * n;
+  const int warp = threadIdx.x >> 5;
+  const signed char* ar = arity + bd.gate_off[b] / 16;
+  double2* gb = gates + bd.gate_off[b];
+  if (threadIdx.x == 0) s_nuc = 0.0;
+  for (int sw = 0; sw < num_sweeps; ++sw) {
+    __syncthreads();
+    if (!active[b]) break;
+    // C|0>
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) psi[i] = make_float4(i == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    for (int j = 0; j < G; ++j) {
+      const int l = L - 1 - j / n, sidx = j % n, k = ar[l * n + sidx];
+      if (!((k == 1) || (k == 2 && sidx <= n - 2))) {
+        if (threadIdx.x == 0) atomicOr(bd.err, KERR_BAD_GATE);
+        continue;
+      }
+      __syncthreads();
+      x_load_gate(gb + ((int64_t)l * n + sidx) * 16, 1 << k, 0, gs);
+      __syncthreads();
+      x_fused_apply(psi, n, sidx, k, gs);
+    }
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) tt[i] = target[bd.vec_off[b] + i];
+    // backward sweep
+    for (int j = 0; j < G; ++j) {
+      const int l = j / n, sidx = n - 1 - j % n, k = ar[l * n + sidx];
+      if (!((k == 1) || (k == 2 && sidx <= n - 2))) {
+        if (threadIdx.x == 0) atomicOr(bd.err, KERR_BAD_GATE);
+        continue;
+      }
+      const int m = 1 << k;
+      double2* gptr = gb + ((int64_t)l * n + sidx) * 16;
+      __syncthreads();
+      x_load_gate(gptr, m, 1, gs);
+      __syncthreads();
+      XA e[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) e[i] = xa_zero();
+      if (k == 2) {
+        const int slo = n - 2 - sidx;
+        const int64_t dlo = (int64_t)1 << slo, dhi = dlo << 1;
+        for (int64_t r = threadIdx.x; r < ipow2(n - 2); r += blockDim.x) {
+          const int64_t i0 = quad_base(r, slo);
+          const int64_t idx[4] = {i0, i0 + dlo, i0 + dhi, i0 + dhi + dlo};
+          xc x[4], y[4], tv[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) x[a] = psi[idx[a]];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            XA acc = xa_zero();
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xa_mac(acc, gs[a * 4 + c], x[c]);
+            y[a] = xa_round(acc);
+            psi[idx[a]] = y[a];
+            tv[a] = tt[idx[a]];
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xa_macc(e[a * 4 + c], tv[a], y[c]);
+        }
+      } else {
+        const int bit = n - 1 - sidx;
+        const int64_t d = (int64_t)1 << bit;
+        for (int64_t r = threadIdx.x; r < ipow2(n - 1); r += blockDim.x) {
+          const int64_t i0 = pair_base(r, bit);
+          const xc x0 = psi[i0], x1 = psi[i0 + d];
+          XA s0 = xa_zero(), s1 = xa_zero();
+          xa_mac(s0, gs[0], x0);
+          xa_mac(s0, gs[1], x1);
+          xa_mac(s1, gs[2], x0);
+          xa_mac(s1, gs[3], x1);
+          const xc y0 = xa_round(s0), y1 = xa_round(s1);
+          psi[i0] = y0;
+          psi[i0 + d] = y1;
+          const xc t0 = tt[i0], t1 = tt[i0 + d];
+          xa_macc(e[0], t0, y0);
+          xa_macc(e[1], t0, y1);
+          xa_macc(e[2], t1, y0);
+          xa_macc(e[3], t1, y1);
+        }
+      }
+      double acc[32];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const double2 dv = xa_to_d(e[i]);
+        acc[2 * i] = dv.x;
+        acc[2 * i + 1] = dv.y;
+      }
+      warp_partial16_f64(acc, &wred[warp][0]);
+      __syncthreads();
+      if (threadIdx.x < 16) {
+        double2 sum = czero();
+        for (int w = 0; w < WARPS; ++w) sum = cadd(sum, wred[w][threadIdx.x]);
+        env[threadIdx.x] = sum;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double2 ee[16], w[16], wprev[16];
+        bool finite = true;
+        for (int i = 0; i < m * m; ++i) {
+          ee[i] = env[i];
+          finite = finite && isfinite(ee[i].x) && isfinite(ee[i].y);
+        }
+        if (!finite) {
+          atomicOr(bd.err, KERR_NONFINITE);
+        } else {
+          for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
+          const double nn = polar_jacobi_pre(ee, m, w, wprev);
+          for (int i = 0; i < m * m; ++i) gptr[i] = cconj(w[i]);
+          s_nuc = nn;
+        }
+      }
+      __syncthreads();
+      // t <- G_new^H t
+      x_load_gate(gptr, m, 1, gs);
+      __syncthreads();
+      x_fused_apply(tt, n, sidx, k, gs);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double f = s_nuc / sqrt(tnorm2[b].x);
+      sweep_fid[(int64_t)b * num_sweeps + sw] = f;
+      sweeps_done[b] = sw + 1;
+      if (stop_fid > 0.0 && f >= stop_fid) active[b] = 0;
+    }
+  }
+}
+
 // ---- launches ---------------------------------------------------------------------------
 
 void launch_x_from_d(const BatchDev& bd, const double2* src, xc* dst, cudaStream_t s) {
@@ -783,4 +972,16 @@ void launch_x_sweep_step(const BatchDev& bd, int step, xc* psi, const xc* t, dou
   qm_note_launch();
   k_x_sweep_step<<<grid_for(bd), BLOCK_THREADS, 0, s>>>(bd, step, psi, t, gates, arity, nlayers, active, partials,
                                                         nuc);
+}
+
+int launch_x_sweep_fused(const BatchDev& bd, int max_n, const xc* target, double2* gates, const signed char* arity,
+                         const int* nlayers, int* active, const double2* tnorm2, int num_sweeps, double stop_fid,
+                         double* sweep_fid, int* sweeps_done, cudaStream_t s) {
+  const size_t smem = 2 * sizeof(xc) * (size_t)ipow2(max_n);
+  cudaError_t e = cudaFuncSetAttribute(k_x_sweep_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  qm_note_launch();
+  k_x_sweep_fused<<<bd.B, BLOCK_THREADS, smem, s>>>(bd, target, gates, arity, nlayers, active, tnorm2, num_sweeps,
+                                                    stop_fid, sweep_fid, sweeps_done);
+  return (int)cudaGetLastError();
 }

@@ -41,5 +41,11 @@ void launch_x_layer_fidelity(const BatchDev& bd, int layer, const xc* work, int 
 
 // (c)/(d) gates and sweeps
 void launch_x_apply_gate(const BatchDev& bd, xc* vec, const GateSel& sel, cudaStream_t s);
+// every sweep of every state in one launch, one block per state (states of
+// at most X_FUSED_MAXN qubits: psi and t in shared memory)
+#define X_FUSED_MAXN 12
+int launch_x_sweep_fused(const BatchDev& bd, int max_n, const xc* target, double2* gates, const signed char* arity,
+                         const int* nlayers, int* active, const double2* tnorm2, int num_sweeps, double stop_fid,
+                         double* sweep_fid, int* sweeps_done, cudaStream_t s);
 void launch_x_sweep_step(const BatchDev& bd, int step, xc* psi, const xc* t, double2* gates, const signed char* arity,
                          const int* nlayers, const int* active, double2* partials, double* nuc, cudaStream_t s);

@@ -1097,6 +1097,12 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   if (rc != QMPRS_OK) return rc;
   launch_fill_int(p->active, p->B, 1, s);
   launch_overlap(p->bd, target, target, p->partials, p->tnorm, s);
+  if (p->max_n <= SWEEP_FUSED_MAXN && !p->prof) {   // every state fits one block's shared memory
+    const int e = launch_sweep_fused(p->bd, p->max_n, target, gates, ar, num_layers, p->active, p->tnorm, num_sweeps,
+                                     stop_fidelity, sweep_fid, sweeps_done, s);
+    if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "k_sweep_fused");
+    return check_kernel_errors(p, s);
+  }
   // group plan of the backward order (the gates' arity does not change
   // between sweeps)
   launch_group_plan(p->bd, p->gd, ar, num_layers, s);

@@ -233,6 +233,13 @@ void launch_cgemm(const float2* A, int64_t lda, const double2* B, int64_t ldb, f
 void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, const int* bonds, int chi,
                          const float2* src, float2* dst_buf, float2* target, cudaStream_t s);
 
+// every sweep of a batch of states of at most SWEEP_FUSED_MAXN qubits in one
+// launch (sweep_fused.cu): one block per state, psi and t in shared memory
+#define SWEEP_FUSED_MAXN 13
+int launch_sweep_fused(const BatchDev& bd, int max_n, const float2* target, double2* gates, const signed char* arity,
+                       const int* nlayers, int* active, const double2* tnorm2, int num_sweeps, double stop_fid,
+                       double* sweep_fid, int* sweeps_done, cudaStream_t s);
+
 // misc
 void qm_note_launch();   // counts every kernel launch the library issues
 void launch_fill_int(int* p, int64_t count, int value, cudaStream_t s);

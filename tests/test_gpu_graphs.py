@@ -45,7 +45,9 @@ def test_graph_replay_is_bit_identical(eng, precision, stop):
     _, before = eng.graph_stats(p)
     runs = [eng.encode(svs, 16, **kw) for _ in range(4)]      # direct, capture, replay, replay
     cached, after = eng.graph_stats(p)
-    assert cached >= 2 and after - before >= 6, (cached, before, after)
+    # the layer stage replays a graph from the third call on; the sweep
+    # stage of states this small is one launch (every sweep in one kernel)
+    assert cached >= 1 and after - before >= 3, (cached, before, after)
     for r in runs:
         for a, b in zip(_fields(r), _fields(ref)):
             assert np.array_equal(a, b)

@@ -55,6 +55,10 @@ int hc_rank_by_cutoff(const double* sq, int n, double cutoff, int max_bond) {
   return rank_by_cutoff(sq, n, cutoff, max_bond);
 }
 
+int hc_rank_from_tails(const double* lsort, int kr, int k, double rest, double total, double cutoff, int max_bond) {
+  return rank_from_tails(lsort, kr, k, rest, total, cutoff, max_bond);
+}
+
 void hc_phase_fix_column(double* v, int n, int ncols, int col) {
   double2 a[64];
   for (int i = 0; i < n * ncols; ++i) a[i] = cd(v[2 * i], v[2 * i + 1]);

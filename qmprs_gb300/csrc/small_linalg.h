@@ -143,6 +143,27 @@ QM_HD int rank_by_cutoff(const double* sq_in, int n, double cutoff, int max_bond
   return keep;
 }
 
+// The same rule when only the largest Kr eigenvalues are known (descending
+// in lsort) and `rest` is the weight of all the others: tail sums are
+// formed from the bottom, rest + sum_{i <= j < Kr} l_j, so that no sum near
+// the total is subtracted from the total; the keep count is capped at K
+// (<= Kr) and by max_bond; total is the trace.  With Kr = n and rest = 0
+// it equals rank_by_cutoff up to the total's rounding.
+QM_HD int rank_from_tails(const double* lsort, int Kr, int K, double rest, double total, double cutoff,
+                          int max_bond) {
+  double tail = rest > 0.0 ? rest : 0.0;
+  for (int i = Kr - 1; i >= K; --i) tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
+  int keep = 0;
+  if (tail > cutoff * total) keep = K;   // tail_from(K): more than K would be kept
+  for (int i = K - 1; i >= 0 && keep == 0; --i) {
+    tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
+    if (tail > cutoff * total) keep = i + 1;
+  }
+  if (keep < 1) keep = 1;
+  if (max_bond > 0 && keep > max_bond) keep = max_bond;
+  return keep;
+}
+
 // v <- v - w * (2 <w, v> / <w, w>)
 QM_HD void householder_apply(const double2* w, double2* v, int n) {
   double2 dot = czero();

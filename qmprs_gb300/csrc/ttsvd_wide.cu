@@ -773,17 +773,7 @@ __global__ void __launch_bounds__(1024) k_bj_finalize(BatchDev bd, int b, int c,
       rest = total;
       for (int i = 0; i < Kr; ++i) rest -= lamK[i];
     }
-    if (rest < 0.0) rest = 0.0;
-    double tail = rest;
-    for (int i = Kr - 1; i >= K; --i) tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
-    int keep = 0;
-    if (tail > cutoff * total) keep = K;   // tail_from(K): more than K would be kept
-    for (int i = K - 1; i >= 0 && keep == 0; --i) {
-      tail += lsort[i] > 0.0 ? lsort[i] : 0.0;
-      if (tail > cutoff * total) keep = i + 1;
-    }
-    if (keep < 1) keep = 1;
-    if (max_bond > 0 && keep > max_bond) keep = max_bond;
+    int keep = rank_from_tails(lsort, Kr, K, rest, total, cutoff, max_bond);
     if (keep > bd.tt_b) keep = bd.tt_b;
     if (c < 30 && keep > (1 << c)) keep = 1 << c;
     bond[c] = keep;

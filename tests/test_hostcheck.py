@@ -29,6 +29,9 @@ def hc():
     lib.hc_complement.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
     lib.hc_rank_by_cutoff.argtypes = [dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.hc_rank_by_cutoff.restype = ctypes.c_int
+    lib.hc_rank_from_tails.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_int]
+    lib.hc_rank_from_tails.restype = ctypes.c_int
     lib.hc_phase_fix_column.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.hc_ran_gate.argtypes = [ctypes.c_int, dp, dp]
     return lib
@@ -357,3 +360,22 @@ def test_preconditioned_polar_null_space_follows_previous(hc, rank, seed):
     w64 = np.zeros((4, 4), np.complex128)
     hc.hc_polar(_p(_c(e)), 4, _p(w64), _p(prev))
     assert np.allclose(w, w64, atol=1e-9)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_rank_from_tails_matches_rsum2(hc, seed):
+    """The blocked eigensolver's rule (only the largest Kr eigenvalues known,
+    the rest as one weight) keeps what quimb's rsum2 rule keeps on the full
+    spectrum: decaying spectra that cross the 1e-10 cutoff, rank-deficient
+    ones, and caps that bind."""
+    rng = np.random.default_rng(seed)
+    n = 200
+    lam = np.sort(10.0 ** rng.uniform(-16, 0, n))[::-1]
+    lam[rng.integers(40, n):] = 0.0                      # a null tail
+    total = float(lam.sum())
+    for K in (20, 60, 120, n):
+        for Kr in sorted({K, min(n, K + 7), n}):
+            rest = float(lam[Kr:].sum())
+            ref = min(cv.rank_by_cutoff(np.sqrt(lam)), K)
+            got = hc.hc_rank_from_tails(_p(np.ascontiguousarray(lam[:Kr])), Kr, K, rest, total, 1e-10, 0)
+            assert got == ref, (K, Kr, got, ref)

@@ -8,8 +8,9 @@
 //   t                  the target;
 //   per gate (backward circuit order)
 //     psi <- G^H psi   peel the gate from the circuit state,
-//     E = sum_rest conj(t[a, rest]) psi[c, rest]   (FP32 per thread, FP64
-//                      across lanes and warps in fixed order),
+//     E = sum_rest conj(t[a, rest]) psi[c, rest]   (FP32 per thread and
+//                      across a warp's lanes, FP64 across the warps, in
+//                      fixed order),
 //     W = polar(E)     thread 0, polar_sweep (FP32 Jacobi, null directions
 //                      towards the current gate), G <- conj(W),
 //     t <- G^H t;
@@ -57,6 +58,27 @@ __device__ __forceinline__ void fused_apply(float2* v, int n, int q, int k, cons
       v[i0 + d] = fmac(fmac(cf(0.f, 0.f), gs[2], x0), gs[3], x1);
     }
   }
+}
+
+// Per-warp sum of 16 complex FP32 accumulators by a fixed FP32 butterfly;
+// lane i < 16 writes entry i in FP64.  A lane holds one to four quads of a
+// state of at most 13 qubits, so the FP32 sum over 32 lanes rounds at
+// about 3e-7 of the entry; the FP64 butterfly it replaces held GB300's two
+// FP64 units for about 1300 warp instructions per gate step.
+__device__ __forceinline__ void warp_partial16_f32(const float2 (&e)[16], double2* out) {
+  const int lane = threadIdx.x & 31;
+  double2 mine = czero();
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    float re = e[i].x, im = e[i].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == i) mine = cd((double)re, (double)im);
+  }
+  if (lane < 16) out[lane] = mine;
 }
 
 __device__ __forceinline__ float2 conj_mul(float2 a, float2 b) {   // conj(a) b
@@ -164,7 +186,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_fused(BatchDev bd, cons
           e[3].y += p3.y;
         }
       }
-      warp_partial16(e, &wred[warp][0]);
+      warp_partial16_f32(e, &wred[warp][0]);
       __syncthreads();
       if (threadIdx.x < 16) {
         double2 sum = czero();

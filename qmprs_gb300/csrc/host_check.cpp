@@ -55,6 +55,8 @@ int hc_rank_by_cutoff(const double* sq, int n, double cutoff, int max_bond) {
   return rank_by_cutoff(sq, n, cutoff, max_bond);
 }
 
+void hc_round_robin_pair(int n, int k, int i, int* p, int* q) { round_robin_pair(n, k, i, p, q); }
+
 int hc_rank_from_tails(const double* lsort, int kr, int k, double rest, double total, double cutoff, int max_bond) {
   return rank_from_tails(lsort, kr, k, rest, total, cutoff, max_bond);
 }

@@ -164,6 +164,23 @@ QM_HD int rank_from_tails(const double* lsort, int Kr, int K, double rest, doubl
   return keep;
 }
 
+// Pair i (0 <= i < n/2) of round k (0 <= k < n-1) of the round-robin
+// tournament over n (even) indices, p < q: index 0 stays, 1..n-1 rotate.
+// The rounds of a sweep are perfect matchings and meet every pair once
+// (Golub & Van Loan, Matrix Computations, 4th ed., sec. 8.5.4).
+QM_HD void round_robin_pair(int n, int k, int i, int* p, int* q) {
+  const int t2 = n - 1 - i;
+  int a = i == 0 ? 0 : 1 + ((i - 1 + k) % (n - 1));
+  int b = 1 + ((t2 - 1 + k) % (n - 1));
+  if (a > b) {
+    const int t = a;
+    a = b;
+    b = t;
+  }
+  *p = a;
+  *q = b;
+}
+
 // v <- v - w * (2 <w, v> / <w, w>)
 QM_HD void householder_apply(const double2* w, double2* v, int n) {
   double2 dot = czero();

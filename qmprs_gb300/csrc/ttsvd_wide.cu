@@ -84,19 +84,9 @@
 #define BJ_EXTRA 32         // ... are refined too, at most this many
 #define BJ_MAX_ROT 0.3       // largest rotation (sin) a refinement step takes per pair
 
-// Pair i of round k of the round-robin tournament over n (even) indices.
-__host__ __device__ inline void bj_pair(int n, int k, int i, int* p, int* q) {
-  const int t2 = n - 1 - i;
-  int a = i == 0 ? 0 : 1 + ((i - 1 + k) % (n - 1));
-  int b = 1 + ((t2 - 1 + k) % (n - 1));
-  if (a > b) {
-    const int t = a;
-    a = b;
-    b = t;
-  }
-  *p = a;
-  *q = b;
-}
+// Pair i of round k of the round-robin tournament over n (even) indices
+// (round_robin_pair, small_linalg.h).
+__host__ __device__ inline void bj_pair(int n, int k, int i, int* p, int* q) { round_robin_pair(n, k, i, p, q); }
 
 // Global index of local index l (0..31) of pair i in round k: the first 16
 // are block p, the next 16 block q.

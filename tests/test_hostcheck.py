@@ -32,6 +32,8 @@ def hc():
     lib.hc_rank_from_tails.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_int]
     lib.hc_rank_from_tails.restype = ctypes.c_int
+    ip = ctypes.POINTER(ctypes.c_int)
+    lib.hc_round_robin_pair.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, ip]
     lib.hc_phase_fix_column.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.hc_ran_gate.argtypes = [ctypes.c_int, dp, dp]
     return lib
@@ -379,3 +381,22 @@ def test_rank_from_tails_matches_rsum2(hc, seed):
             ref = min(cv.rank_by_cutoff(np.sqrt(lam)), K)
             got = hc.hc_rank_from_tails(_p(np.ascontiguousarray(lam[:Kr])), Kr, K, rest, total, 1e-10, 0)
             assert got == ref, (K, Kr, got, ref)
+
+
+@pytest.mark.parametrize("n", [2, 4, 32, 128, 2048 // 16])
+def test_round_robin_rounds_are_matchings_meeting_every_pair_once(hc, n):
+    """The tournament of the blocked Jacobi (blocks of a round, indices of a
+    32 x 32 subproblem's inner rounds): each round pairs every index once,
+    and a sweep of n - 1 rounds meets every pair exactly once."""
+    seen = set()
+    p, q = ctypes.c_int(), ctypes.c_int()
+    for k in range(n - 1):
+        used = set()
+        for i in range(n // 2):
+            hc.hc_round_robin_pair(n, k, i, ctypes.byref(p), ctypes.byref(q))
+            assert 0 <= p.value < q.value < n
+            assert p.value not in used and q.value not in used
+            used |= {p.value, q.value}
+            seen.add((p.value, q.value))
+        assert len(used) == n
+    assert len(seen) == n * (n - 1) // 2

@@ -236,6 +236,22 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target, void* gates, const
                           int* sweeps_done, void* stream);
 
 /*
+ * (d) Gate environments at a fixed circuit.  One backward pass over every
+ * gate, as a sweep makes it but without replacing any gate: env (the gate
+ * store's layout and size, complex128) receives at each gate's slot the
+ * m x m environment E with <target|C|0> = sum_{a,c} G[a,c] E[a,c] for that
+ * gate G; entries outside the gates are zero.  E is the derivative of the
+ * circuit overlap with respect to the gate's entries, which trains the
+ * learned warm start on circuit fidelity.  Fast precision only
+ * (QMPRS_ERR_INVALID for an exact plan).  Synchronises the stream.
+ * Replaces: the environment contraction of
+ * Sequential._sweep_unitary_layers (qmprs/synthesis/mps_encoding/
+ * sequential.py:463-477) with the update left out.
+ */
+int qmprs_layer_environments(qmprs_plan_t p, const void* target, const void* gates, const int8_t* arity,
+                             const int* num_layers, void* env, void* stream);
+
+/*
  * Dense circuit state C|0...0> of the stored layers (circuit order = reverse
  * generation order).
  * Replaces: Sequential._tensor_network_from_unitary_layers(...).to_dense()
@@ -329,6 +345,22 @@ int qmprs_mlp_col_sum(const float* X, int B, int N, float* out, void* stream);
  */
 int qmprs_mlp_adam(float* W, const float* G, int gT, float* m, float* v, int rows, int cols, float lr, float b1,
                    float b2, float eps, int step, float wd, void* Wb, void* WTb, void* stream);
+
+/*
+ * Circuit-overlap loss of the warm start.  For rows r < rows: slots[r] and
+ * kind[r] as in qmprs_mlp_project; `gates` holds the projected outputs and
+ * `env` their environments from qmprs_layer_environments (both complex128,
+ * the gate store's layout).  fid[r] = |f|^2 tinv[r] with
+ * f = sum_ac U[a,c] E[a,c] the state's circuit overlap (tinv[r] =
+ * 1 / <t|t> of the row's state).  dY (B x 32 fp32, also bf16 and
+ * transposed bf16 32 x ldt) = the gradient of -gscale fid[r] with respect
+ * to the network output, through the tangent map of the polar factor at U;
+ * rows rows..B-1 get zero gradient.  No reference counterpart (the
+ * reference has no learned part).
+ */
+int qmprs_mlp_overlap_grad(const void* env, const void* gates, const int64_t* slots, const int8_t* kind,
+                           const float* tinv, int rows, int B, float gscale, float* fid, float* dY, void* dYb,
+                           void* dYT, int ldt, void* stream);
 
 /*
  * Project network outputs to gates: row r of Y (4 x 4 complex, interleaved

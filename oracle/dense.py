@@ -315,6 +315,26 @@ def sweep(target: np.ndarray, n: int, layers: list[Layer], mode: str = "canonica
     return layers, nuc / float(np.linalg.norm(target))
 
 
+def environments(target: np.ndarray, n: int, layers: list[Layer]) -> list[np.ndarray]:
+    """Every gate's environment at the fixed circuit, in circuit order.
+
+    The backward pass of ``sweep`` (sequential.py:452-505) with the update
+    left out: the circuit state peeled gate by gate and the target carried
+    back through the same gates, so <target|C|0> = sum(G * E) for each
+    gate G and its environment E.
+    """
+    gates = circuit_gates(layers)
+    psi = circuit_state(layers, n)
+    t = target.astype(np.complex128, copy=True)
+    out = []
+    for _, _, _, q, g in reversed(gates):
+        k = 1 if g.shape[0] == 2 else 2
+        psi = apply_gate(psi, n, g.conj().T, q)
+        out.append(environment(t, psi, n, q, k))
+        t = apply_gate(t, n, g.conj().T, q)
+    return out[::-1]
+
+
 def iter_dioall(target: np.ndarray, n: int, num_layers: int, sweeps_per_layer: int,
                 mode: str = "canonical") -> tuple[list[Layer], list[list[float]]]:
     """Iter-DiOall schedule (arXiv:2209.00595; the reference documents it as

@@ -15,6 +15,10 @@ checker the GPU kernels of ``qmprs_gb300/csrc/mlp.cu`` are held to:
                        per sample (4 x 4 complex, row-major, interleaved)
                        and its gradient;
 * ``backward``         parameter gradients of the weighted mean loss.
+* ``overlap_grad``     the circuit-overlap loss: per gate row, the state's
+                       fidelity |sum U*E|^2 tinv and the gradient of
+                       -gscale times it with respect to the network output,
+                       through the tangent map of the polar factor at U.
 
 The GELU is the tanh form 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).
 """
@@ -99,3 +103,39 @@ def init_params(dims, seed: int):
         w = (rng.standard_normal((dims[i + 1], dims[i])) * np.sqrt(2.0 / dims[i])).astype(np.float32)
         out.append((w, np.zeros(dims[i + 1], np.float32)))
     return out
+
+
+def polar_factor(y: np.ndarray) -> np.ndarray:
+    """Unitary polar factor W V^H of y = W S V^H."""
+    w, _, vh = np.linalg.svd(y)
+    return w @ vh
+
+
+def overlap_grad(env: np.ndarray, gates: np.ndarray, kind: np.ndarray, tinv: np.ndarray, gscale: float):
+    """Circuit-overlap loss rows (the restatement of ``k_mlp_overlap_grad``).
+
+    env, gates: (rows x 16) complex128 slots (m x m row-major in the first
+    m*m entries, m = 2 for kind 1, else 4).  With f = sum_ac U[a,c] E[a,c]
+    (the state's overlap <t|C|0>) the row's fidelity is F = |f|^2 tinv.  The
+    gradient of -gscale F with respect to U, in the complex form
+    d/dRe + i d/dIm, is G = -2 gscale tinv f conj(E); the polar factor's
+    tangent map at a unitary U carries it to the network output as
+    U skew(U^H G), skew(X) = (X - X^H) / 2.  Returns (F, dY) with dY
+    (rows x 32) float64, interleaved re/im, zero beyond m*m entries.
+    """
+    rows = env.shape[0]
+    fid = np.zeros(rows)
+    dy = np.zeros((rows, 32))
+    for r in range(rows):
+        m = 2 if kind[r] == 1 else 4
+        u = gates[r, : m * m].reshape(m, m)
+        e = env[r, : m * m].reshape(m, m)
+        f = np.sum(u * e)
+        fid[r] = abs(f) ** 2 * tinv[r]
+        g = -2.0 * gscale * tinv[r] * f * np.conj(e)
+        x = u.conj().T @ g
+        gy = u @ (0.5 * (x - x.conj().T))
+        flat = gy.reshape(-1)
+        dy[r, 0 : 2 * m * m : 2] = flat.real
+        dy[r, 1 : 2 * m * m : 2] = flat.imag
+    return fid, dy

@@ -61,6 +61,8 @@ SIGNATURES: dict[str, tuple] = {
                                             _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_optimize_layers": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int,
                                              ctypes.c_double, _c_void_p, _c_void_p, _c_void_p]),
+    "qmprs_layer_environments": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                                                _c_void_p]),
     "qmprs_circuit_state": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_overlap": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_apply_layer": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int, ctypes.c_int,
@@ -79,6 +81,9 @@ SIGNATURES: dict[str, tuple] = {
                                       ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_int, ctypes.c_float, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_mlp_project": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
+    "qmprs_mlp_overlap_grad": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_float, _c_void_p, _c_void_p, _c_void_p,
+                                              _c_void_p, ctypes.c_int, _c_void_p]),
 }
 
 _lib = None

@@ -1234,6 +1234,57 @@ int qmprs_optimize_layers(qmprs_plan_t p, const void* target_, void* gates_, con
   return check_kernel_errors(p, s);
 }
 
+// One sweep's backward pass with the update left out: the same kernels
+// (fused for small states, rebuild + group passes otherwise) write every
+// gate's environment to env and keep the gates.
+int qmprs_layer_environments(qmprs_plan_t p, const void* target_, const void* gates_, const int8_t* arity,
+                             const int* num_layers, void* env_, void* stream) {
+  if (!p || !target_ || !gates_ || !arity || !num_layers || !env_) return QMPRS_ERR_INVALID;
+  if (p->precision == QMPRS_PRECISION_EXACT)
+    return set_err(p->h, QMPRS_ERR_INVALID, "qmprs_layer_environments runs in the fast precision only");
+  cudaStream_t s = (cudaStream_t)stream;
+  const float2* target = (const float2*)target_;
+  // the environment mode reads the gates and never writes them
+  double2* gates = const_cast<double2*>((const double2*)gates_);
+  double2* env = (double2*)env_;
+  const signed char* ar = (const signed char*)arity;
+  CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(env, 0, sizeof(double2) * (size_t)p->gate_total, s));
+  int max_gates = 0;
+  int rc = read_max_gates(p, num_layers, s, &max_gates);
+  if (rc != QMPRS_OK) return rc;
+  launch_fill_int(p->active, p->B, 1, s);
+  launch_overlap(p->bd, target, target, p->partials, p->tnorm, s);
+  if (p->max_n <= SWEEP_FUSED_MAXN) {
+    const int e = launch_sweep_fused(p->bd, p->max_n, target, gates, ar, num_layers, p->active, p->tnorm, 1, 0.0,
+                                     nullptr, nullptr, s, env);
+    if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "k_sweep_fused");
+    return check_kernel_errors(p, s);
+  }
+  launch_group_plan(p->bd, p->gd, ar, num_layers, s);
+  std::vector<int> ngroups(p->B, 0), nrgroups(p->B, 0);
+  CK(cudaMemcpyAsync(ngroups.data(), p->d_ngroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(nrgroups.data(), p->d_nrgroups, sizeof(int) * p->B, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int max_groups = 0, max_rpasses = 0;
+  for (int b = 0; b < p->B; ++b) {
+    max_groups = std::max(max_groups, ngroups[b]);
+    max_rpasses = std::max(max_rpasses, (nrgroups[b] + 1) / 2);
+  }
+  float2* psi = p->S0;
+  float2* t = p->S1;
+  launch_set_zero_state(p->bd, psi, p->active, s);
+  for (int r = 0; r < max_rpasses; ++r)
+    launch_rebuild_pass(p->bd, p->gd, r, psi, gates, ar, num_layers, p->active, s);
+  for (int g = 0; g < max_groups; ++g) {
+    const int e = launch_group_pass(p->bd, p->gd, g, psi, g <= 1 ? target : t, t, gates, ar, num_layers, p->active,
+                                    p->tnorm, s);
+    if (e != 0) return cuda_fail(p->h, (cudaError_t)e, "cudaFuncSetAttribute(k_group_pass)");
+    launch_group_polar(p->bd, p->gd, g, gates, ar, num_layers, p->active, p->nuc, s, env);
+  }
+  return check_kernel_errors(p, s);
+}
+
 int qmprs_circuit_state(qmprs_plan_t p, const void* gates, const int8_t* arity, const int* num_layers, void* out,
                         void* stream) {
   if (!p || !gates || !arity || !num_layers || !out) return QMPRS_ERR_INVALID;

@@ -177,8 +177,11 @@ int layer_pass_bound(int max_n);
 int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi, const float2* z_in, float2* z_out,
                       const double2* gates, const signed char* arity, const int* nlayers, const int* active,
                       const double2* znorm, cudaStream_t s);
+// env_out: write each gate's environment there (gate-store layout) and
+// leave the gates unchanged (one pass at a fixed circuit)
 void launch_group_polar(const BatchDev& bd, const GroupDev& gd, int g, double2* gates, const signed char* arity,
-                        const int* nlayers, const int* active, double* nuc, cudaStream_t s);
+                        const int* nlayers, const int* active, double* nuc, cudaStream_t s,
+                        double2* env_out = nullptr);
 void launch_sweep_finish(int B, int sweep, int num_sweeps, const double* nuc, const double2* tnorm2,
                          double* sweep_fid, int* sweeps_done, int* active, double stop_fid,
                          int* num_active, cudaStream_t s);
@@ -238,7 +241,7 @@ void launch_mps_contract(const BatchDev& bd, int step, const double2* tensors, c
 #define SWEEP_FUSED_MAXN 13
 int launch_sweep_fused(const BatchDev& bd, int max_n, const float2* target, double2* gates, const signed char* arity,
                        const int* nlayers, int* active, const double2* tnorm2, int num_sweeps, double stop_fid,
-                       double* sweep_fid, int* sweeps_done, cudaStream_t s);
+                       double* sweep_fid, int* sweeps_done, cudaStream_t s, double2* env_out = nullptr);
 
 // misc
 void qm_note_launch();   // counts every kernel launch the library issues

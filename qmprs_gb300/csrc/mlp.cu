@@ -15,6 +15,9 @@
 //                activation and its transpose; or FP32 split-K partials.
 // k_mlp_loss     phase-invariant gate loss |M - e^{i phi} U|_F^2 minimised
 //                over phi, and its gradient.
+// k_mlp_overlap_grad  circuit-overlap loss: the gradient of a state's
+//                fidelity |<t|C|0>|^2 / <t|t> with respect to each
+//                projected gate, from the gate's environment.
 // k_act_back     dZ = dH * GELU'(Z), BF16 and transposed BF16.
 // k_col_sum      bias gradients (column sums in fixed order).
 // k_splitk_sum   split-K reduction in fixed order.
@@ -306,6 +309,64 @@ __global__ void k_mlp_loss(const float* Y, const float* U, const float* w, int B
   }
 }
 
+// Circuit-overlap loss.  Row r's gate U (the projected network output, in
+// its slot of the gate store) and its environment E give the state's overlap
+// f = sum_ac U[a,c] E[a,c] (the same for every gate of the state, up to
+// rounding) and fidelity F = |f|^2 tinv[r], written to fid[r].  The gradient
+// of -gscale F with respect to U (complex form d/dRe + i d/dIm) is
+// G = -2 gscale tinv[r] f conj(E); it reaches the network output Y through
+// the tangent map of the polar factor at U: dY = U skew(U^H G),
+// skew(X) = (X - X^H) / 2 (the Hermitian part of U^H dY does not move the
+// polar factor).  Rows rows..B-1 (padding) get zero gradient.
+__global__ void k_mlp_overlap_grad(const double2* env, const double2* gates, const int64_t* slots,
+                                   const signed char* kind, const float* tinv, int rows, int B, float gscale,
+                                   float* fid, float* dY, __nv_bfloat16* dYb, __nv_bfloat16* dYT, int ldt) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < B; s += gridDim.x * blockDim.x) {
+    float out[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) out[i] = 0.f;
+    if (s < rows) {
+      const int m = kind[s] == 1 ? 2 : 4;
+      const double2* u = gates + slots[s] * 16;
+      const double2* e = env + slots[s] * 16;
+      double2 f = czero();
+      for (int i = 0; i < m * m; ++i) f = cadd(f, cmul(u[i], e[i]));
+      const double ti = (double)tinv[s];
+      fid[s] = (float)((f.x * f.x + f.y * f.y) * ti);
+      const double c = -2.0 * (double)gscale * ti;
+      double2 G[16], X[16];
+      for (int i = 0; i < m * m; ++i) {
+        const double2 fe = cmul(f, cconj(e[i]));
+        G[i] = cd(c * fe.x, c * fe.y);
+      }
+      for (int a = 0; a < m; ++a)   // X = U^H G
+        for (int b2 = 0; b2 < m; ++b2) {
+          double2 acc = czero();
+          for (int k = 0; k < m; ++k) acc = cadd(acc, cmul(cconj(u[k * m + a]), G[k * m + b2]));
+          X[a * m + b2] = acc;
+        }
+      for (int a = 0; a < m; ++a)   // dY = U skew(X)
+        for (int b2 = 0; b2 < m; ++b2) {
+          double2 acc = czero();
+          for (int k = 0; k < m; ++k) {
+            const double2 xk = X[k * m + b2], xt = cconj(X[b2 * m + k]);
+            acc = cadd(acc, cmul(u[a * m + k], cd(0.5 * (xk.x - xt.x), 0.5 * (xk.y - xt.y))));
+          }
+          out[2 * (a * m + b2)] = (float)acc.x;
+          out[2 * (a * m + b2) + 1] = (float)acc.y;
+        }
+    } else {
+      fid[s] = 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      dY[(int64_t)s * 32 + i] = out[i];
+      dYb[(int64_t)s * 32 + i] = __float2bfloat16_rn(out[i]);
+      dYT[(int64_t)i * ldt + s] = __float2bfloat16_rn(out[i]);
+    }
+  }
+}
+
 // dZ = dH * GELU'(Z) for [B x N]; BF16 copy and transposed BF16 copy [N x ldt]
 __global__ void k_act_back(const float* dH, const float* Z, int B, int N, float* dZ, __nv_bfloat16* dZb,
                            __nv_bfloat16* dZT, int ldt) {
@@ -482,6 +543,19 @@ int qmprs_mlp_adam(float* W, const float* G, int gT, float* m, float* v, int row
     k_adam<<<grid1((int64_t)rows * cols, 256), 256, 0, (cudaStream_t)stream>>>(
         W, G, gT, m, v, rows, cols, lr, b1, b2, eps, bc1, bc2, wd, (__nv_bfloat16*)Wb, (__nv_bfloat16*)WTb);
   }
+  return cudaGetLastError() == cudaSuccess ? QMPRS_OK : QMPRS_ERR_CUDA;
+}
+
+int qmprs_mlp_overlap_grad(const void* env, const void* gates, const int64_t* slots, const int8_t* kind,
+                           const float* tinv, int rows, int B, float gscale, float* fid, float* dY, void* dYb,
+                           void* dYT, int ldt, void* stream) {
+  if (!env || !gates || !slots || !kind || !tinv || !fid || !dY || !dYb || !dYT || rows < 0 || B < rows ||
+      B <= 0 || ldt < B)
+    return QMPRS_ERR_INVALID;
+  qm_note_launch();
+  k_mlp_overlap_grad<<<grid1(B, 128), 128, 0, (cudaStream_t)stream>>>(
+      (const double2*)env, (const double2*)gates, slots, (const signed char*)kind, tinv, rows, B, gscale, fid, dY,
+      (__nv_bfloat16*)dYb, (__nv_bfloat16*)dYT, ldt);
   return cudaGetLastError() == cudaSuccess ? QMPRS_OK : QMPRS_ERR_CUDA;
 }
 

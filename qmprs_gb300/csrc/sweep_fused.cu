@@ -16,6 +16,10 @@
 //     t <- G^H t;
 //   the sweep fidelity nuc / ||target||, the sweep count, the stop at
 //   stop_fidelity.
+// With env_out set, one pass computes every gate's environment at the fixed
+// circuit instead: E is written to the gate's slot of env_out (the gate
+// store's layout, <target|C|0> = sum_ac G[a, c] E[a, c] for every gate),
+// the gates stay as they are and no fidelity is written.
 // On a 1024-amplitude state the grouped sweep is bound by launches and its
 // FP64 window algebra (about 130 launches per sweep); here a step is a few
 // block-wide passes over shared memory and one FP32 polar factor.
@@ -89,7 +93,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_fused(BatchDev bd, cons
                                                                const signed char* arity, const int* nlayers,
                                                                int* active, const double2* tnorm2, int num_sweeps,
                                                                double stop_fid, double* sweep_fid,
-                                                               int* sweeps_done) {
+                                                               int* sweeps_done, double2* env_out) {
   extern __shared__ float2 fsm[];
   __shared__ float2 gs[16];
   __shared__ double2 wred[WARPS][16];
@@ -203,6 +207,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_fused(BatchDev bd, cons
         }
         if (!finite) {
           atomicOr(bd.err, KERR_NONFINITE);
+        } else if (env_out) {
+          double2* eo = env_out + bd.gate_off[b] + ((int64_t)l * n + sidx) * 16;
+          for (int i = 0; i < m * m; ++i) eo[i] = ee[i];
         } else {
           for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
           const double nn = polar_sweep(ee, m, w, wprev);
@@ -216,7 +223,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_fused(BatchDev bd, cons
       fused_apply(tt, n, sidx, k, gs);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !env_out) {
       const double f = s_nuc / sqrt(tnorm2[b].x);
       sweep_fid[(int64_t)b * num_sweeps + sw] = f;
       sweeps_done[b] = sw + 1;
@@ -227,12 +234,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS) k_sweep_fused(BatchDev bd, cons
 
 int launch_sweep_fused(const BatchDev& bd, int max_n, const float2* target, double2* gates, const signed char* arity,
                        const int* nlayers, int* active, const double2* tnorm2, int num_sweeps, double stop_fid,
-                       double* sweep_fid, int* sweeps_done, cudaStream_t s) {
+                       double* sweep_fid, int* sweeps_done, cudaStream_t s, double2* env_out) {
   const size_t smem = 2 * sizeof(float2) * (size_t)ipow2(max_n);
   cudaError_t e = cudaFuncSetAttribute(k_sweep_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
   qm_note_launch();
   k_sweep_fused<<<bd.B, BLOCK_THREADS, smem, s>>>(bd, target, gates, arity, nlayers, active, tnorm2, num_sweeps,
-                                                  stop_fid, sweep_fid, sweeps_done);
+                                                  stop_fid, sweep_fid, sweeps_done, env_out);
   return (int)cudaGetLastError();
 }

@@ -962,7 +962,7 @@ __device__ void m_cols(double2* M, int D, const double2* G, int k, int h, int l)
 
 __global__ void __launch_bounds__(POLAR_THREADS) k_group_polar(BatchDev bd, GroupDev gd, int g, double2* gates,
                                                                const signed char* arity, const int* nlayers,
-                                                               const int* active, double* nuc) {
+                                                               const int* active, double* nuc, double2* env_out) {
   __shared__ double2 M[GMM];
   __shared__ double2 env[16];
   for (int b = blockIdx.x; b < bd.B; b += gridDim.x) {
@@ -1033,6 +1033,9 @@ __global__ void __launch_bounds__(POLAR_THREADS) k_group_polar(BatchDev bd, Grou
         for (int i = 0; i < m * m; ++i) keep[i] = gptr[i];
         if (!finite) {
           atomicOr(bd.err, KERR_NONFINITE);
+        } else if (env_out) {   // environment at the fixed circuit: the gate stays
+          double2* eo = env_out + bd.gate_off[b] + slot * 16;
+          for (int i = 0; i < m * m; ++i) eo[i] = e[i];
         } else {
           for (int i = 0; i < m * m; ++i) wprev[i] = cconj(gptr[i]);
           const double nn = polar_sweep(e, m, w, wprev);
@@ -1108,7 +1111,7 @@ int launch_group_pass(const BatchDev& bd, const GroupDev& gd, int g, float2* psi
 }
 
 void launch_group_polar(const BatchDev& bd, const GroupDev& gd, int g, double2* gates, const signed char* arity,
-                        const int* nlayers, const int* active, double* nuc, cudaStream_t s) {
+                        const int* nlayers, const int* active, double* nuc, cudaStream_t s, double2* env_out) {
   qm_note_launch();
-  k_group_polar<<<bd.B, POLAR_THREADS, 0, s>>>(bd, gd, g, gates, arity, nlayers, active, nuc);
+  k_group_polar<<<bd.B, POLAR_THREADS, 0, s>>>(bd, gd, g, gates, arity, nlayers, active, nuc, env_out);
 }

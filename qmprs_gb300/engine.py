@@ -295,6 +295,17 @@ class Engine:
                                                          float(stop_fidelity), _ptr(sf), _ptr(sd), sp))
         return sf, sd
 
+    def environments(self, p: Plan, target, gates, arity, nl, env: torch.Tensor | None = None,
+                     stream=None) -> torch.Tensor:
+        """Every gate's environment at the fixed circuit (no update), in the
+        gate store's layout (complex128 as float64 pairs): at each slot the
+        m x m E with <target|C|0> = sum(G * E) for that gate G."""
+        if env is None:
+            env = torch.empty(p.gate_elems * 2, dtype=torch.float64, device="cuda")
+        self.hd.check(self.lib.qmprs_layer_environments(p.p, _ptr(target), _ptr(gates), _ptr(arity), _ptr(nl),
+                                                        _ptr(env), self._sp(stream)))
+        return env
+
     def stage_circuit(self, p: Plan, gates, arity, nl, stream=None, reuse: str = "") -> torch.Tensor:
         sp = self._sp(stream)
         circ = p.buf(reuse + "_circ", p.vec_elems * 2, p.vdtype) if reuse else p.vec()

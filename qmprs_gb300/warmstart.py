@@ -268,6 +268,28 @@ class WarmStartMLP:
         wsum = float(weight.sum().item())
         _check(self.lib.qmprs_mlp_loss(_p(buf.Y), _p(U), _p(w), B, 1.0 / wsum, _p(buf.loss), _p(buf.dY),
                                        _p(buf.dYb), _p(buf.dYT), B, _sp(stream)), "qmprs_mlp_loss")
+        grads = self._backprop(buf, B, stream)
+        loss = float((buf.loss[:rows].sum() / wsum).item())
+        return loss, grads
+
+    def backward_overlap(self, env: torch.Tensor, gates: torch.Tensor, slots: torch.Tensor, kind: torch.Tensor,
+                         tinv: torch.Tensor, num_states: int, stream=None, grads: bool = True):
+        """Circuit-fidelity loss on the last forward (train=True) batch, whose
+        rows were projected into `gates` (qmprs_mlp_project) and whose
+        environments at those gates are `env` (qmprs_layer_environments).
+        The loss is the batch's mean infidelity 1 - |<t|C|0>|^2 / <t|t> over
+        its `num_states` states; returns (per-row fidelity, gradients or
+        None when grads is False)."""
+        rows = int(slots.shape[0])
+        B = _pad128(rows)
+        buf = self._buf(B)
+        _check(self.lib.qmprs_mlp_overlap_grad(_p(env), _p(gates), _p(slots), _p(kind), _p(tinv), rows, B,
+                                               1.0 / float(num_states), _p(buf.loss), _p(buf.dY), _p(buf.dYb),
+                                               _p(buf.dYT), B, _sp(stream)), "qmprs_mlp_overlap_grad")
+        return buf.loss[:rows], (self._backprop(buf, B, stream) if grads else None)
+
+    def _backprop(self, buf: _Buf, B: int, stream=None):
+        """Parameter gradients from dY (and its bf16 copies) in `buf`."""
         nl = len(DIMS) - 1
         grads = [None] * nl
         ksplit = 512 if B > 512 else 0
@@ -296,8 +318,7 @@ class WarmStartMLP:
             # dZb holds dZ_j; the next iteration's first GEMM reads it before
             # act_back overwrites it (stream order)
             d_bf, d_w = buf.dZb, nout
-        loss = float((buf.loss[:rows].sum() / wsum).item())
-        return loss, grads
+        return grads
 
     def adam(self, grads, lr: float, b1=0.9, b2=0.999, eps=1e-8, wd=0.0, stream=None) -> None:
         self.step_count += 1
@@ -370,3 +391,94 @@ def _sp(stream) -> ctypes.c_void_p:
     if stream is None:
         stream = torch.cuda.current_stream()
     return ctypes.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+# ---- training on the circuit overlap ------------------------------------------------
+
+@dataclass
+class OverlapBatch:
+    """One plan's states, prepared for training on the circuit overlap: the
+    targets, the analytic layers (features and fallback), the block rows."""
+    plan: object
+    target: torch.Tensor
+    analytic: torch.Tensor      # the analytic gate store (float64 pairs)
+    work: torch.Tensor          # gate store the predictions are projected into
+    env: torch.Tensor           # environments at `work`
+    arity: torch.Tensor
+    nl: torch.Tensor
+    x: torch.Tensor             # features (rows x 256 float32)
+    slots: torch.Tensor         # int64 gate-store slot per row
+    kind: torch.Tensor          # int8 qubits per row's gate
+    state: torch.Tensor         # int64 state index per row
+    tinv: torch.Tensor          # float32 1 / <t|t> per row
+    num_states: int
+
+
+def overlap_batch(eng, p, target: torch.Tensor, gates: torch.Tensor, arity: torch.Tensor,
+                  nl: torch.Tensor) -> OverlapBatch:
+    """Prepare a plan whose analytic layers are in `gates` (kept unchanged)."""
+    dev = gates.device
+    nlh = nl.cpu().numpy()
+    blocks = block_index(p.nqubits, nlh)
+    x = features(gates, p.gate_off, p.nqubits, nlh, blocks, dev)
+    tn = eng.overlap(p, target, target)[0::2]
+    st = torch.as_tensor(blocks[:, 0], device=dev)
+    return OverlapBatch(
+        plan=p, target=target, analytic=gates.clone(), work=gates.clone(), env=torch.empty_like(gates),
+        arity=arity, nl=nl, x=x, slots=torch.as_tensor(slots_of(p.gate_off, p.nqubits, blocks), device=dev),
+        kind=torch.as_tensor(block_kind(p.nqubits, blocks), device=dev), state=st,
+        tinv=(1.0 / tn)[st].float().contiguous(), num_states=p.B)
+
+
+def _state_mean(ob: OverlapBatch, rows: torch.Tensor) -> torch.Tensor:
+    """Mean over each state's rows (float64, one entry per state)."""
+    s = torch.zeros(ob.num_states, dtype=torch.float64, device=rows.device)
+    c = torch.zeros_like(s)
+    s.index_add_(0, ob.state, rows.double())
+    c.index_add_(0, ob.state, torch.ones_like(rows, dtype=torch.float64))
+    return s / c.clamp(min=1)
+
+
+def overlap_step(eng, model: WarmStartMLP, ob: OverlapBatch, lr: float | None, stream=None) -> torch.Tensor:
+    """One Adam step on the batch's mean infidelity 1 - |<t|C|0>|^2 / <t|t>
+    of the predicted layers (no step when lr is None); returns each state's
+    fidelity before the step."""
+    rows = int(ob.slots.shape[0])
+    y = model.forward(ob.x, train=lr is not None, stream=stream)
+    ob.work.copy_(ob.analytic)   # null directions complete towards the analytic gate
+    _check(model.lib.qmprs_mlp_project(_p(y), rows, _p(ob.slots), _p(ob.kind), _p(ob.work), _sp(stream)),
+           "qmprs_mlp_project")
+    eng.environments(ob.plan, ob.target, ob.work, ob.arity, ob.nl, env=ob.env, stream=stream)
+    fid, grads = model.backward_overlap(ob.env, ob.work, ob.slots, ob.kind, ob.tinv, ob.num_states,
+                                        stream=stream, grads=lr is not None)
+    if lr is not None:
+        model.adam(grads, lr, stream=stream)
+    return _state_mean(ob, fid)
+
+
+def train_overlap(eng, model: WarmStartMLP, batches: list, epochs: int, lr: float = 2e-4, log=None,
+                  keep_best: bool = True) -> list:
+    """Train on the circuit overlap: every epoch takes one step per batch
+    (cosine-decayed learning rate).  Returns the mean fidelity of the
+    predicted layers over all states per epoch (measured before each step of
+    the epoch), then that of the final parameters.  With keep_best the
+    parameters of the best entry are restored at the end (the first entry is
+    the analytic layers' fidelity, so training never ends below it)."""
+    hist, best_f, best_p = [], -1.0, None
+    total = epochs * len(batches)
+    for ep in range(epochs + 1):
+        snap = model.params() if keep_best else None
+        fs = []
+        for i, ob in enumerate(batches):
+            k = ep * len(batches) + i
+            lr_k = None if ep == epochs else lr * 0.5 * (1 + np.cos(np.pi * k / total))
+            fs.append(overlap_step(eng, model, ob, lr_k))
+        hist.append(float(torch.cat(fs).mean().item()))
+        if keep_best and hist[-1] > best_f:
+            best_f, best_p = hist[-1], snap
+        if log:
+            log(f"epoch {ep}: mean fidelity of the predicted layers {hist[-1]:.5f}")
+    if keep_best and best_p is not None and best_f > hist[-1]:
+        model.load_params(best_p)
+    model.check_errors()
+    return hist

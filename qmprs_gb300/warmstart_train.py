@@ -2,13 +2,17 @@
 
     python -m qmprs_gb300.warmstart_train --train-states 2048 --out ws.npz
 
-1. Training pairs: seeded states of a family (--family random_mps: random
+1. Training states: seeded states of a family (--family random_mps: random
    MPS with bond uniform in {8, 16, 32}; gmm: Gaussian mixtures on the
    amplitude grid), qubits uniform in --qmin..--qmax, go through the plain
-   GPU path: analytic
-   layers (--layers) then --sweeps sweeps.  Every two-qubit block gives one
-   pair (features of the analytic layers, the block's optimised gate).
-2. The network is trained with the library's tensor-core kernels.
+   GPU path's analytic layers (--layers).
+2. --objective overlap (the default): the network is trained on the circuit
+   fidelity |<t|C|0>|^2 / <t|t> of its predicted layers.  Every step projects
+   the predictions to unitaries, computes every gate's environment at that
+   circuit (qmprs_layer_environments), turns them into the gradient
+   (qmprs_mlp_overlap_grad) and back-propagates it through the library's
+   tensor-core kernels.  --objective gates: the earlier per-gate loss against
+   the gates after --sweeps sweeps of the plain path (one pair per block).
 3. Evaluation on held-out states (--eval-qubits qubits): the plain path
    (analytic layers, then sweeps) against the warm start (predicted layers,
    then sweeps), fidelity |<target|C|0>| after every sweep, from the same
@@ -79,6 +83,24 @@ def make_pairs(eng, ns, bonds, layers, sweeps, chi, seed, batch=256, log=print, 
     return torch.cat(xs), torch.cat(ys)
 
 
+def overlap_batches(eng, ns, bonds, layers, chi, seed, batch=256, log=print, family="random_mps"):
+    """Training batches for the circuit-overlap objective: targets and
+    analytic layers of the given states, one plan per `batch` states."""
+    out = []
+    t0 = time.perf_counter()
+    for k, (nb, bb) in enumerate(_batches(ns, bonds, batch)):
+        sv = states(eng, family, nb, bb, seed + k)
+        p = eng.plan(nb, layers, chi)
+        _, _, target = eng.stage_mps(p, sv, chi)
+        gates, arity, nl, _ = eng.stage_layers(p, target, layers, 1 - 1e-6)
+        out.append(W.overlap_batch(eng, p, target, gates, arity, nl))
+        del sv
+    torch.cuda.synchronize()
+    log(f"overlap batches: {sum(int(b.slots.shape[0]) for b in out)} gates of {len(ns)} states "
+        f"in {time.perf_counter() - t0:.1f} s")
+    return out
+
+
 def evaluate(eng, model, ns, bonds, layers, sweeps, chi, seed, batch=256, family="random_mps"):
     """Per-sweep fidelities (B x sweeps) of the plain and the warm-started path."""
     plain, warm, init_p, init_w = [], [], [], []
@@ -117,23 +139,36 @@ def main() -> None:
     ap.add_argument("--chi", type=int, default=64)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=4096)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=None, help="default 2e-4 (overlap), 1e-3 (gates)")
     ap.add_argument("--eval-states", type=int, default=256)
     ap.add_argument("--eval-qubits", type=int, default=20)
     ap.add_argument("--eval-sweeps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default="")
     ap.add_argument("--family", default="random_mps", choices=["random_mps", "gmm"])
+    ap.add_argument("--objective", default="overlap", choices=["overlap", "gates"])
+    ap.add_argument("--state-batch", type=int, default=256, help="states per plan (overlap objective)")
     args = ap.parse_args()
+    if args.lr is None:
+        args.lr = 2e-4 if args.objective == "overlap" else 1e-3
     eng = E.engine()
     rng = np.random.default_rng(args.seed)
     ns = [int(x) for x in rng.integers(args.qmin, args.qmax + 1, size=args.train_states)]
     bonds = [int(x) for x in rng.choice([8, 16, 32], size=args.train_states)]
-    x, y = make_pairs(eng, ns, bonds, args.layers, args.sweeps, args.chi, seed=args.seed * 1000,
-                      family=args.family)
     model = W.WarmStartMLP(seed=args.seed)
-    t0 = time.perf_counter()
-    hist = model.train(x, y, epochs=args.epochs, batch=args.batch, lr=args.lr, log=print)
+    if args.objective == "overlap":
+        batches = overlap_batches(eng, ns, bonds, args.layers, args.chi, seed=args.seed * 1000,
+                                  batch=args.state_batch, family=args.family)
+        pairs = sum(int(b.slots.shape[0]) for b in batches)
+        t0 = time.perf_counter()
+        hist = W.train_overlap(eng, model, batches, epochs=args.epochs, lr=args.lr, log=print)
+        del batches
+    else:
+        x, y = make_pairs(eng, ns, bonds, args.layers, args.sweeps, args.chi, seed=args.seed * 1000,
+                          family=args.family)
+        pairs = int(x.shape[0])
+        t0 = time.perf_counter()
+        hist = model.train(x, y, epochs=args.epochs, batch=args.batch, lr=args.lr, log=print)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     if args.out:
@@ -144,9 +179,10 @@ def main() -> None:
                               seed=args.seed * 1000 + 777777, family=args.family)
     thr = float(np.median(fp[:, -1]))
     line = {
-        "family": args.family, "target_sweeps": args.sweeps,
-        "pairs": int(x.shape[0]), "train_states": args.train_states, "epochs": args.epochs,
-        "train_seconds": train_s, "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+        "family": args.family, "objective": args.objective, "target_sweeps": args.sweeps,
+        "pairs": pairs, "train_states": args.train_states, "epochs": args.epochs, "lr": args.lr,
+        "train_seconds": train_s, "history_first": hist[0], "history_last": hist[-1],
+        "history_best": max(hist) if args.objective == "overlap" else min(hist),
         "eval_states": args.eval_states, "eval_qubits": args.eval_qubits, "layers": args.layers,
         "init_fidelity_plain": float(ip.mean()), "init_fidelity_warm": float(iw.mean()),
         "fidelity_per_sweep_plain": [float(v) for v in fp.mean(axis=0)],

@@ -65,3 +65,39 @@ def test_gelu_grad(z):
     eps = 1e-6
     fd = (OM.gelu(z + eps) - OM.gelu(z - eps)) / (2 * eps)
     assert abs(fd - OM.gelu_grad(z)) < 1e-8
+
+
+@pytest.mark.parametrize("m", [2, 4])
+def test_overlap_grad_matches_finite_differences(m):
+    """The circuit-overlap loss row: fid = |sum U*E|^2 tinv, and dY is the
+    derivative of -gscale fid(polar(Y)) at a unitary Y = U (finite
+    differences along random complex directions, both signs of the step)."""
+    rng = np.random.default_rng(5 + m)
+    z = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+    u = OM.polar_factor(z)
+    e = 0.4 * (rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m)))
+    tinv, gscale = 0.8, 0.25
+    env = np.zeros((1, 16), complex)
+    gates = np.zeros((1, 16), complex)
+    env[0, : m * m] = e.reshape(-1)
+    gates[0, : m * m] = u.reshape(-1)
+    kind = np.array([1 if m == 2 else 2])
+    fid, dy = OM.overlap_grad(env, gates, kind, np.array([tinv]), gscale)
+    assert np.isclose(fid[0], abs(np.sum(u * e)) ** 2 * tinv)
+    assert np.all(dy[0, 2 * m * m:] == 0)
+    g = dy[0, : 2 * m * m : 2] + 1j * dy[0, 1 : 2 * m * m : 2]
+
+    def loss(y):
+        return -gscale * tinv * abs(np.sum(OM.polar_factor(y) * e)) ** 2
+
+    h = 1e-6
+    for _ in range(6):
+        d = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+        num = (loss(u + h * d) - loss(u - h * d)) / (2 * h)
+        ana = float(np.real(np.sum(np.conj(g) * d.reshape(-1))))
+        assert abs(num - ana) < 1e-6 * max(1.0, abs(ana)), (num, ana)
+    # a Hermitian stretch U (I + H) leaves the polar factor, so the gradient
+    # has no component along it
+    hm = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+    d = u @ (hm + hm.conj().T)
+    assert abs(np.real(np.sum(np.conj(g) * d.reshape(-1)))) < 1e-12

@@ -209,3 +209,28 @@ def test_iter_dioi_oracle_sweeps_the_newest_layer_only():
     for a, b in zip(l0, l1):
         for (s1, e1, g1), (s2, e2, g2) in zip(a, b):
             assert (s1, e1) == (s2, e2) and all(np.allclose(x, y) for x, y in zip(g1, g2))
+
+
+def test_environments_give_the_overlap_and_do_not_depend_on_their_gate():
+    """<t|C|0> = sum(G * E_G) for every gate of a fixed circuit, and E_G does
+    not depend on G: a replaced gate G' gives the overlap sum(G' * E_G)."""
+    n, L = 6, 3
+    t = S.uniform_complex(n, 3)
+    t = t / np.linalg.norm(t)
+    layers, _ = D.get_unitary_layers(t, n, L)
+    envs = D.environments(t, n, layers)
+    gates = D.circuit_gates(layers)
+    assert len(envs) == len(gates)
+    f = np.vdot(t, D.circuit_state(layers, n))
+    for (_, _, _, _, g), e in zip(gates, envs):
+        assert abs(np.sum(g * e) - f) < 1e-12
+    rng = np.random.default_rng(1)
+    for idx in (0, len(gates) // 2, len(gates) - 1):
+        li, bi, ti, q, g = gates[idx]
+        m = g.shape[0]
+        z = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+        w, _, vh = np.linalg.svd(z)
+        mod = [[(s, e, list(gs)) for s, e, gs in layer] for layer in layers]
+        mod[li][bi][2][ti] = w @ vh
+        f2 = np.vdot(t, D.circuit_state(mod, n))
+        assert abs(np.sum((w @ vh) * envs[idx]) - f2) < 1e-12

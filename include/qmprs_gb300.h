@@ -347,6 +347,16 @@ int qmprs_mlp_adam(float* W, const float* G, int gT, float* m, float* v, int row
                    float b2, float eps, int step, float wd, void* Wb, void* WTb, void* stream);
 
 /*
+ * Test of the bounded tensor-core completion wait of qmprs_gemm_bf16: one
+ * block allocates tensor memory and waits on an mbarrier at which nothing
+ * will arrive.  After its limit (about one second of wall time) the wait
+ * gives up, bit 16 of `err` (a device int) is raised and the tensor memory
+ * is freed, as qmprs_gemm_bf16 does after a timeout; the context stays
+ * usable.  No reference counterpart (error handling of this library).
+ */
+int qmprs_tc_wait_selftest(int* err, void* stream);
+
+/*
  * Circuit-overlap loss of the warm start.  For rows r < rows: slots[r] and
  * kind[r] as in qmprs_mlp_project; `gates` holds the projected outputs and
  * `env` their environments from qmprs_layer_environments (both complex128,

@@ -81,6 +81,7 @@ SIGNATURES: dict[str, tuple] = {
                                       ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_int, ctypes.c_float, _c_void_p, _c_void_p, _c_void_p]),
     "qmprs_mlp_project": (ctypes.c_int, [_c_void_p, ctypes.c_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
+    "qmprs_tc_wait_selftest": (ctypes.c_int, [_c_void_p, _c_void_p]),
     "qmprs_mlp_overlap_grad": (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_float, _c_void_p, _c_void_p, _c_void_p,
                                               _c_void_p, ctypes.c_int, _c_void_p]),

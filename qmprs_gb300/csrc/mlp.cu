@@ -44,6 +44,7 @@
 #define MLP_SMEM_B 32768
 #define MLP_SMEM_REQ (96 * 1024)
 #define MLP_WAIT_LIMIT (1 << 22)
+#define MLP_WAIT_NS 1000000000ull   // and at most one second of wall time
 
 enum { MLP_ACT_NONE = 0, MLP_ACT_GELU = 1 };
 
@@ -125,8 +126,17 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, int count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // Bounded wait for the phase with the given parity; false on timeout.
+// try_wait may suspend the thread for a system-dependent time, so the
+// bound is both an iteration count and a wall-clock limit.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
   for (int it = 0; it < MLP_WAIT_LIMIT; ++it) {
     uint32_t done;
     asm volatile(
@@ -136,6 +146,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
         : "r"(smem_u32(mbar)), "r"(parity)
         : "memory");
     if (done) return true;
+    if (globaltimer_ns() - t0 > MLP_WAIT_NS) return false;
   }
   return false;
 }
@@ -246,6 +257,39 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) k_gemm_tc(GemmArgs g) {
       }
     }
   }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(MLP_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// Test of the bounded completion wait: one block allocates tensor memory as
+// k_gemm_tc does and waits on an mbarrier at which no tcgen05.commit will
+// arrive (nothing is issued).  The wait gives up after its limit, the
+// timeout bit is raised and the tensor memory is freed: the path k_gemm_tc
+// takes after a timeout, without a fault and with the context usable.
+__global__ void __launch_bounds__(MLP_THREADS, 1) k_tc_wait_selftest(int* err) {
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_sh;
+  const int warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_sh)),
+                 "r"(MLP_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_sh;
+  const bool ok = __syncthreads_and(mbar_wait(&mbar, 0u) ? 1 : 0) != 0;
+  if (!ok && threadIdx.x == 0) atomicOr(err, KERR_TC_TIMEOUT);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -543,6 +587,13 @@ int qmprs_mlp_adam(float* W, const float* G, int gT, float* m, float* v, int row
     k_adam<<<grid1((int64_t)rows * cols, 256), 256, 0, (cudaStream_t)stream>>>(
         W, G, gT, m, v, rows, cols, lr, b1, b2, eps, bc1, bc2, wd, (__nv_bfloat16*)Wb, (__nv_bfloat16*)WTb);
   }
+  return cudaGetLastError() == cudaSuccess ? QMPRS_OK : QMPRS_ERR_CUDA;
+}
+
+int qmprs_tc_wait_selftest(int* err, void* stream) {
+  if (!err) return QMPRS_ERR_INVALID;
+  qm_note_launch();
+  k_tc_wait_selftest<<<1, MLP_THREADS, 0, (cudaStream_t)stream>>>(err);
   return cudaGetLastError() == cudaSuccess ? QMPRS_OK : QMPRS_ERR_CUDA;
 }
 

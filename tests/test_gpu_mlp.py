@@ -42,6 +42,23 @@ def test_gemm_tc_matches_torch(ws, M, N, K, ksplit):
     assert rel < 1e-5, float(rel)
 
 
+def test_tc_wait_timeout_raises_the_error_bit(ws):
+    """A completion wait that nothing completes (no MMA issued) gives up
+    after about a second, raises error bit 16 and frees the tensor memory:
+    the GEMM that follows allocates it again and is exact."""
+    import time
+    lib = ws.N.load()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    assert lib.qmprs_tc_wait_selftest(ws._p(err), ws._sp(None)) == 0
+    torch.cuda.synchronize()
+    waited = time.perf_counter() - t0
+    assert int(err.item()) == 16
+    assert waited < 10.0, waited
+    test_gemm_tc_matches_torch(ws, 128, 32, 64, 0)
+
+
 def test_gemm_epilogue_bias_gelu_transpose(ws):
     rng = np.random.default_rng(3)
     M, N, K = 256, 64, 128

@@ -476,8 +476,11 @@ __device__ __forceinline__ void pass_flush_tc(const float (&acc)[2][4][4], doubl
 }
 
 // Tile loads: 8-byte cp.async copies straight into swizzled shared memory,
-// one commit group per tile, so the next tile streams in while the current
-// one is processed.
+// one commit group per tile.  The rebuild pass keeps two tiles in flight
+// (the next streams in while the current one is processed); the group pass
+// holds one (x, z) tile pair per block and overlaps one block's loads with
+// the arithmetic of the other three blocks on its SM (double-buffered at
+// three blocks per SM it was slower).
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");

@@ -2,10 +2,9 @@
 
 The reference initialises every unitary layer analytically (Ran's
 construction, ``qmprs/primitives/mps.py:849-891``) and then sweeps.  Here a
-small network predicts, for every gate of the layers, the gate the sweeps
-converge to, from the gate's analytic initial value, the analytic gates
-around it (two sites either side, the same site in the neighbouring
-layers) and a position embedding.  The predicted matrices are projected to
+small network predicts every gate of the layers from the gate's analytic
+initial value, the analytic gates around it (two sites either side, the
+same site in the neighbouring layers) and a position embedding.  The predicted matrices are projected to
 unitaries (polar factor, null space completed towards the analytic gate) and
 replace the analytic ones; all gates are replaced together because the
 converged gates are one solution up to gauge, and mixing solutions breaks
@@ -16,11 +15,23 @@ that misses the target fidelity continues with the plain method).
 Network: 128 -> 256 -> 256 -> 256 -> 32, GELU, BF16 weights and
 activations, FP32 accumulation, residual output (the prediction is the
 block's analytic gate plus the network's correction, so an untrained network
-reproduces the analytic layers), trained with Adam on the phase-invariant
-gate loss min_phi |Y - e^{i phi} U|_F^2.  Every matmul runs on the tensor cores
-through ``qmprs_gemm_bf16`` (tcgen05.mma); loss, activation backward, bias
-gradients and the optimiser are the library's own kernels.  PyTorch only
-allocates device memory and gathers features.
+reproduces the analytic layers), trained with Adam on one of two losses:
+
+* the circuit fidelity |<t|C|0>|^2 / <t|t> of the predicted layers
+  (``train_overlap``): every gate's environment at the projected circuit
+  (``qmprs_layer_environments``, the sweep's own kernels without the update)
+  is the derivative of the overlap with respect to that gate, and
+  ``qmprs_mlp_overlap_grad`` carries it through the polar projection to the
+  network output;
+* the phase-invariant gate loss min_phi |Y - e^{i phi} U|_F^2 against the
+  gates after the plain path's sweeps (``WarmStartMLP.train``), which learns
+  the gate map but loses circuit fidelity: per-gate errors add up coherently
+  over the circuit.
+
+Every matmul runs on the tensor cores through ``qmprs_gemm_bf16``
+(tcgen05.mma); losses, activation backward, bias gradients and the optimiser
+are the library's own kernels.  PyTorch only allocates device memory and
+gathers features.
 """
 
 from __future__ import annotations

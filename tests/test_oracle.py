@@ -234,3 +234,40 @@ def test_environments_give_the_overlap_and_do_not_depend_on_their_gate():
         mod[li][bi][2][ti] = w @ vh
         f2 = np.vdot(t, D.circuit_state(mod, n))
         assert abs(np.sum((w @ vh) * envs[idx]) - f2) < 1e-12
+
+
+def test_overlap_gradient_is_the_derivative_of_circuit_fidelity():
+    """End to end on a circuit: the environment of a gate and the overlap
+    loss's gradient (oracle.mlp.overlap_grad, the restatement of the GPU
+    kernel) give the derivative of the circuit fidelity |<t|C|0>|^2 / <t|t>
+    when that gate is replaced by the polar factor of U + h D."""
+    from oracle import mlp as OM
+    n, L = 5, 2
+    t = S.uniform_complex(n, 9)          # not normalised: <t|t> enters as tinv
+    layers, _ = D.get_unitary_layers(t / np.linalg.norm(t), n, L)
+    envs = D.environments(t, n, layers)
+    gates = D.circuit_gates(layers)
+    tinv = 1.0 / float(np.vdot(t, t).real)
+    rng = np.random.default_rng(4)
+    for idx in (1, len(gates) - 2):
+        li, bi, ti, q, g = gates[idx]
+        m = g.shape[0]
+        env = np.zeros((1, 16), complex)
+        gr = np.zeros((1, 16), complex)
+        env[0, : m * m] = envs[idx].reshape(-1)
+        gr[0, : m * m] = g.reshape(-1)
+        fid, dy = OM.overlap_grad(env, gr, np.array([1 if m == 2 else 2]), np.array([tinv]), 1.0)
+        grad = dy[0, : 2 * m * m : 2] + 1j * dy[0, 1 : 2 * m * m : 2]   # of -F
+
+        def fidelity(y):
+            mod = [[(s, e, list(gs)) for s, e, gs in layer] for layer in layers]
+            mod[li][bi][2][ti] = OM.polar_factor(y)
+            return abs(np.vdot(t, D.circuit_state(mod, n))) ** 2 * tinv
+
+        assert abs(fidelity(g) - fid[0]) < 1e-12
+        h = 1e-6
+        for _ in range(3):
+            d = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+            num = (fidelity(g + h * d) - fidelity(g - h * d)) / (2 * h)
+            ana = -float(np.real(np.sum(np.conj(grad) * d.reshape(-1))))
+            assert abs(num - ana) < 1e-6 * max(1.0, abs(ana)), (num, ana)
